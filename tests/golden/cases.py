@@ -1,0 +1,157 @@
+"""Case specifications shared by the golden-fixture generator and the tests.
+
+A case is a plain dict: beam parameters, an element list, the number of
+turns and what to record.  ``make_golden.py`` builds the PyHEADTAIL
+reference objects from it; ``oracle/cases.py`` builds the oracle objects;
+the GPU tests build ``pyheadtail_gb300`` objects.  All three read the same
+dict, so a fixture is only as trustworthy as the builders agreeing on it.
+
+Sizes are small so that the committed fixtures stay around a megabyte.
+"""
+import numpy as np
+
+C_SPS = 6911.5038378975451   # circumference used by the reference's tests
+GAMMA = 27.7
+Z_CUTS = (-0.69, 0.69)        # fixed +-3 sigma_z cuts for sigma_z = 0.23 m
+
+
+def _alpha_c(Q_s=0.017, beta_z=230., gamma=GAMMA, C=C_SPS):
+    # beta_z = |eta| C / (2 pi Q_s) with eta = alpha_c - gamma**-2 > 0
+    return beta_z * 2 * np.pi * Q_s / C + gamma**-2
+
+
+ALPHA_C = _alpha_c()
+
+
+def beam_params(n, seed, **kw):
+    p = dict(n=n, seed=seed, gamma=GAMMA, circumference=C_SPS,
+             intensity=2.5e11, epsn_x=2.5e-6, epsn_y=2.5e-6, beta_x=50.,
+             beta_y=50., alpha_x=0., alpha_y=0., sigma_z=0.23, sigma_dp=1e-3)
+    p.update(kw)
+    return p
+
+
+def smooth_transverse(Q_x=20.13, Q_y=20.18, beta=50., chroma=None,
+                      amplitude=None, n_segments=1, C=C_SPS):
+    s = list(np.arange(0, n_segments + 1) * C / n_segments)
+    m = n_segments + 1
+    return dict(type='transverse', s=s, alpha_x=[0.] * m, beta_x=[beta] * m,
+                D_x=[0.] * m, alpha_y=[0.] * m, beta_y=[beta] * m,
+                D_y=[0.] * m, accQ_x=Q_x, accQ_y=Q_y, chroma=chroma,
+                amplitude=amplitude)
+
+
+def rf(h=(4620,), V=(4.5e6,), dphi=(0.,), alpha=ALPHA_C, p_increment=0.,
+       D_x=0., D_y=0., shrink_transverse=True):
+    return dict(type='rf', h=list(h), V=list(V), dphi=list(dphi),
+                alpha=[alpha], p_increment=p_increment, D_x=D_x, D_y=D_y,
+                shrink_transverse=shrink_transverse)
+
+
+def linear_map(Q_s=0.017, alpha=ALPHA_C, D_x=0., D_y=0.):
+    return dict(type='linear_map', Q_s=Q_s, alpha=[alpha], D_x=D_x, D_y=D_y)
+
+
+def slicer(n_slices, z_cuts=Z_CUTS, n_sigma_z=None):
+    return dict(n_slices=n_slices,
+                z_cuts=None if z_cuts is None else list(z_cuts),
+                n_sigma_z=n_sigma_z)
+
+
+def resonator(R=10e6, f=1e9, Q=1., n_turns_wake=1, kind='circular'):
+    return dict(type='resonator', kind=kind, R=R, f=f, Q=Q,
+                n_turns_wake=n_turns_wake)
+
+
+def resistive_wall(b=0.02, L=C_SPS, sigma=5.8e7, dt_min=1e-12,
+                   n_turns_wake=1, kind='circular'):
+    return dict(type='resistive_wall', kind=kind, b=b, L=L, sigma=sigma,
+                dt_min=dt_min, n_turns_wake=n_turns_wake)
+
+
+def wake(sl, *sources):
+    return dict(type='wake', slicer=sl, sources=list(sources))
+
+
+def probe(sl, statistics=('mean_x', 'mean_y')):
+    """Not an element of the reference: records a SliceSet of the beam in
+    its current state (index, counts, statistics) without changing it."""
+    return dict(type='probe', slicer=sl, statistics=list(statistics))
+
+
+# the C1 and C2 workloads at fixture size (full sizes are in bench.py)
+CASES = {
+    'transverse_linear': dict(
+        beam=beam_params(1000, 11), n_turns=3,
+        elements=[smooth_transverse()]),
+    'transverse_chroma_amp': dict(
+        beam=beam_params(1000, 12), n_turns=3,
+        elements=[smooth_transverse(chroma=[5., 5.],
+                                    amplitude=[1e-11, 1e-11, -5e-12])]),
+    'transverse_segments_dispersion': dict(
+        beam=beam_params(1000, 13), n_turns=3,
+        elements=[dict(type='transverse', s=[0., 1000., 3500., C_SPS],
+                       alpha_x=[0.3, -1.2, 0.7, 0.3],
+                       beta_x=[50., 80., 20., 50.],
+                       D_x=[2.0, 0.5, 1.1, 2.0],
+                       alpha_y=[-0.4, 0.9, -0.2, -0.4],
+                       beta_y=[40., 25., 70., 40.],
+                       D_y=[0., 0.3, 0.0, 0.],
+                       accQ_x=[0., 4.2, 13.6, 20.13],
+                       accQ_y=[0., 6.1, 11.9, 20.18],
+                       chroma=[[3., 120.], [-2., 40., 9000.]],
+                       amplitude=[2e-11, -1e-11, 4e-12])]),
+    'linear_map': dict(
+        beam=beam_params(1000, 14), n_turns=3,
+        elements=[linear_map()]),
+    'rf_single': dict(
+        beam=beam_params(1000, 15), n_turns=3, elements=[rf()]),
+    'rf_double_harmonic': dict(
+        beam=beam_params(1000, 16), n_turns=3,
+        elements=[rf(h=(4620, 4 * 4620), V=(4.5e6, 0.45e6),
+                     dphi=(0., np.pi))]),
+    'rf_accelerating': dict(
+        beam=beam_params(1000, 17), n_turns=3,
+        elements=[smooth_transverse(), rf(p_increment=1e-21,
+                                          D_x=0.7, D_y=0.)]),
+    'slicer_fixed': dict(
+        beam=beam_params(1000, 18), n_turns=1,
+        elements=[probe(slicer(50), ['mean_x', 'mean_y', 'mean_z', 'mean_xp',
+                                     'mean_yp', 'mean_dp', 'sigma_x',
+                                     'sigma_z', 'epsn_x', 'eff_epsn_y',
+                                     'epsn_z']),
+                  probe(slicer(7, z_cuts=(-0.31, 0.05))),
+                  probe(slicer(13, z_cuts=(0.2, -0.2))),
+                  probe(slicer(20, z_cuts=None, n_sigma_z=3)),
+                  probe(slicer(16, z_cuts=None))]),
+    'wake_resonator': dict(
+        beam=beam_params(1000, 19), n_turns=3,
+        elements=[smooth_transverse(), linear_map(),
+                  wake(slicer(50), resonator())]),
+    'wake_multiturn': dict(
+        beam=beam_params(1000, 20), n_turns=6,
+        elements=[smooth_transverse(chroma=[2., 2.]), rf(),
+                  wake(slicer(40), resonator(),
+                       resistive_wall(n_turns_wake=4))]),
+    'wake_dynamic_cuts': dict(
+        beam=beam_params(1000, 21), n_turns=3,
+        elements=[smooth_transverse(), rf(),
+                  wake(slicer(30, z_cuts=None, n_sigma_z=4),
+                       resonator(R=10.2e6, f=1.3e9),
+                       resistive_wall(n_turns_wake=3))]),
+    'wake_plates': dict(
+        beam=beam_params(1000, 22), n_turns=3,
+        elements=[smooth_transverse(), linear_map(),
+                  wake(slicer(25), resonator(kind='parallel_horizontal'),
+                       resonator(R=3e6, f=0.6e9, Q=0.5,
+                                 kind='longitudinal'))]),
+    'c1_full': dict(
+        beam=beam_params(1000, 0), n_turns=5,
+        elements=[smooth_transverse(), linear_map(),
+                  wake(slicer(50), resonator())]),
+    'c2_full': dict(
+        beam=beam_params(1000, 1), n_turns=5,
+        elements=[smooth_transverse(chroma=[5., 5.],
+                                    amplitude=[1e-11, 1e-11, -5e-12]),
+                  rf(), wake(slicer(200), resonator())]),
+}
