@@ -1,0 +1,284 @@
+/*
+ * pyheadtail_gb300.h -- C ABI of the GB300 (sm_103a) single-bunch turn loop.
+ *
+ * The library replaces the per-particle arithmetic of PyHEADTAIL's turn loop
+ * (v1.16.5) behind plain C entry points: device pointers, sizes and POD
+ * parameter blocks, no torch or C++ types.  Every call is asynchronous on the
+ * caller's CUDA stream (passed as void*, a cudaStream_t), never allocates
+ * device memory (all buffers belong to the caller) and returns an int status:
+ *   0      success
+ *   < 0    argument error detected on the host before any launch
+ *          (PHK_E* below); the message is available from phk_last_error()
+ *   > 0    never returned by a call; device-side error words are written to
+ *          the caller's status buffer where an entry point takes one.
+ *
+ * Citations are path:line in the PyHEADTAIL source tree.
+ *
+ * The reference's own native seam for the GPU path is a ctypes binding of
+ * raw device pointers + lengths with no error reporting
+ * (PyHEADTAIL/gpu/thrust_interface.py:5-30, 233-269); the entry points below
+ * take its place for the hot path, and the PyHEADTAIL-shaped Python classes
+ * in pyheadtail_gb300/ drive them.
+ */
+#ifndef PYHEADTAIL_GB300_H
+#define PYHEADTAIL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHK_ABI_VERSION 1
+
+/* status codes */
+#define PHK_OK 0
+#define PHK_ENULL (-1)      /* a required pointer is NULL                  */
+#define PHK_ESIZE (-2)      /* a size / count is out of range              */
+#define PHK_EALIGN (-3)     /* a pointer is not aligned for its dtype      */
+#define PHK_EPARAM (-4)     /* a parameter block is inconsistent           */
+#define PHK_ECUDA (-5)      /* the CUDA runtime reported a launch error    */
+#define PHK_EWORKSPACE (-6) /* a caller workspace is too small             */
+
+/* coordinate storage types */
+#define PHK_F64 0 /* plain form: FP64 coordinates, FP64 arithmetic          */
+#define PHK_F32 1 /* precision form: FP32 coordinates, see DESIGN notes     */
+
+/* limits of the parameter blocks */
+#define PHK_MAX_OPS 12
+#define PHK_MAX_DETUNERS 6
+#define PHK_MAX_POLY 8
+#define PHK_MAX_KICKS 8
+#define PHK_MAX_SLICES 4096
+
+/* coordinate indices (phk_kick_set.target / .quad) */
+#define PHK_X 0
+#define PHK_XP 1
+#define PHK_Y 2
+#define PHK_YP 3
+#define PHK_Z 4
+#define PHK_DP 5
+
+/* ---- particle coordinates: Particles SoA, particles/particles.py:16-57,
+ *      217-229.  Six device arrays of n elements of `dtype`.             */
+typedef struct phk_coords {
+    void *x, *xp, *y, *yp, *z, *dp;
+    int64_t n;
+    int32_t dtype; /* PHK_F64 | PHK_F32 */
+    int32_t reserved;
+} phk_coords;
+
+/* ---- uniform-bin slicer: UniformBinSlicer.compute_sliceset_kwargs,
+ *      particles/slicing.py:599-615.
+ * The slice index of a particle is the reference's
+ *     int32(floor((z - tail) / width)),  width = (head - tail) / n_slices.
+ * `edges` holds, in the coordinate dtype, the n_slices+1 exact lower
+ * boundaries e_k = min{ z : floor((z - tail)/width) >= k } (computed by the
+ * host from that very formula); a particle is inside the cuts iff
+ * e_0 <= z < e_S and its index is the k with e_k <= z < e_{k+1}.  For
+ * width < 0 (tail > head, slicing.py:334-337) the tables are built for -z
+ * and `negate` is 1.  `tail`/`width` are the reference's unmirrored values,
+ * used only for particles outside the cuts when an index array is written.
+ */
+typedef struct phk_slicer {
+    int32_t n_slices;
+    int32_t negate;
+    double tail;      /* z_cut_tail                                      */
+    double width;     /* slice width (may be negative)                   */
+    double est_tail;  /* mirrored tail (for the first index estimate)    */
+    double est_inv_w; /* 1 / |width|                                     */
+    const void *edges; /* device, n_slices + 1 entries of the coords dtype */
+} phk_slicer;
+
+/* ---- element programs --------------------------------------------------
+ * A program is the element sequence of one (part of a) turn, applied to
+ * every particle in one pass.  Parameters are host-computed FP64 scalars
+ * following the reference formulas (see each kind).                       */
+#define PHK_OP_TRANSVERSE 1   /* TransverseSegmentMap.track, transverse_tracking.py:138-196 */
+#define PHK_OP_DRIFT 2        /* Drift.track, longitudinal_tracking.py:107-111            */
+#define PHK_OP_RF_KICK 3      /* Kick.track_*, longitudinal_tracking.py:183-203           */
+#define PHK_OP_LINEAR_LONG 4  /* LinearMap.track_*, longitudinal_tracking.py:731-759      */
+#define PHK_OP_SCALE_TRANS 5  /* RFSystems._shrink_transverse_emittance, :546-554         */
+
+/* op flags */
+#define PHK_FLAG_DISPERSION 1 /* subtract / add D * dp around the op      */
+#define PHK_FLAG_DETUNED 2    /* transverse: per-particle phase advance   */
+#define PHK_FLAG_SHRINK 4     /* drift: beta_ratio != 1                   */
+#define PHK_FLAG_PHI_OFFSET 8 /* rf kick: add phi_offset                  */
+#define PHK_FLAG_PHI_LOCK 16  /* rf kick: add _phi_lock                   */
+#define PHK_FLAG_P_INC 32     /* rf kick: subtract p_increment            */
+
+/*
+ * phk_op.p layout per kind (all FP64):
+ *  TRANSVERSE, not detuned: p[0..7]  = M00 M01 M10 M11 M22 M23 M32 M33
+ *  TRANSVERSE, detuned:     p[0..7]  = I00 I01 I10 I11 I22 I23 I32 I33
+ *                           p[8..15] = J00 J01 J10 J11 J22 J23 J32 J33
+ *                           p[20], p[21] = dQ_x, dQ_y;  p[22] = 2*pi
+ *                           ij_mask bit b set <=> entry b of (I..., J...) != 0
+ *                           detuners det[det_begin .. det_begin+det_count)
+ *  TRANSVERSE, either:      p[16..19] = D_x_s0 D_x_s1 D_y_s0 D_y_s1
+ *  DRIFT:        p[0] = beta_ratio, p[1] = eta0 (alpha_0 - gamma^-2), p[2] = length
+ *  RF_KICK:      p[0] = harmonic, p[1] = 2*pi, p[2] = circumference,
+ *                p[3] = phi_offset, p[4] = _phi_lock, p[5] = |q| V / (beta c),
+ *                p[6] = p0 before, p[7] = p_increment, p[8] = p0 after,
+ *                p[9] = D_x, p[10] = D_y
+ *  LINEAR_LONG:  p[0] = cos(2 pi Q_s), p[1] = sin(2 pi Q_s), p[2] = longfac,
+ *                p[3] = D_x, p[4] = D_y
+ *  SCALE_TRANS:  p[0] = sqrt(betagamma_old / betagamma_new)
+ */
+typedef struct phk_op {
+    int32_t kind;
+    int32_t flags;
+    int32_t det_begin;
+    int32_t det_count;
+    int32_t ij_mask;
+    int32_t reserved;
+    double p[24];
+} phk_op;
+
+/* detuners: ChromaticitySegment.detune (trackers/detuners.py:64-98) and
+ * AmplitudeDetuningSegment.detune (:128-151).
+ *  CHROMA: Horner coefficients c[0..nx-1] (x) and c[8..8+ny-1] (y), lowest
+ *          order first, i.e. detune = (c0 + (c1 + ...)*dp)*dp; zx / zy extra
+ *          factors of dp (the reference's order > 3 polyval path prepends
+ *          one zero coefficient per call, detuners.py:95-97).
+ *  AMPLITUDE: c[0..9] = dapp_x, dapp_y, dapp_xy, dapp_yx,
+ *             (1+ax^2)/bx, 2 ax, bx, (1+ay^2)/by, 2 ay, by;  c[10] = p0    */
+#define PHK_DET_CHROMA 1
+#define PHK_DET_AMPLITUDE 2
+typedef struct phk_detuner {
+    int32_t kind;
+    int32_t nx, ny;
+    int32_t zx, zy;
+    int32_t reserved;
+    double c[16];
+} phk_detuner;
+
+typedef struct phk_program {
+    int32_t n_ops;
+    int32_t n_det;
+    phk_op op[PHK_MAX_OPS];
+    phk_detuner det[PHK_MAX_DETUNERS];
+} phk_program;
+
+/* ---- wake kicks applied to particles: DipoleWakeKickX/Y.apply
+ *      (impedances/wake_kicks.py:207-260), QuadrupoleWakeKick* (:284-361),
+ *      ConstantWakeKickZ (:185-202).  For every particle inside the cuts of
+ *      `slicer`, in order k = 0..n_kicks-1:
+ *          target += kick_k[idx]            (quad[k] < 0)
+ *          target += kick_k[idx] * quad     (quad[k] = PHK_X | PHK_Y)
+ *      kick_k are device arrays of n_slices entries of the coords dtype.  */
+typedef struct phk_kick_set {
+    phk_slicer slicer;
+    int32_t n_kicks;
+    int32_t target[PHK_MAX_KICKS];
+    int32_t quad[PHK_MAX_KICKS];
+    const void *kick[PHK_MAX_KICKS];
+} phk_kick_set;
+
+/* ---- per-slice accumulation (Slicer.slice + add_statistics for the
+ *      dipole moments: slicing.py:348-381, 443-470; stats.pyx:192-253).
+ * Each of the `grid` CTAs writes its per-slice count / sum x / sum y to
+ * partials[q * n_slices * grid + s * grid + cta] (q = 0,1,2); use
+ * phk_track_grid() for `grid` and size partials >= 3 * n_slices * grid.
+ * idx_out (optional, int32[n]) receives the reference's slice index of
+ * every particle (outside particles included; NaN -> INT32_MIN).        */
+typedef struct phk_accum {
+    phk_slicer slicer;
+    double *partials;
+    int64_t partials_len;
+    int32_t *idx_out;
+    int32_t grid;
+    int32_t reserved;
+} phk_accum;
+
+/* ---- wake convolution: WakeKick._accumulate_source_signal + _wake_factor
+ *      (wake_kicks.py:66-73, 118-139) with _convolution_numpy (:87-116) or
+ *      _convolution_dot_product (:75-85).
+ * moments: device ring [ring_len][3][n_slices] FP64 of (count,
+ *          count*mean_x, count*mean_y) per stored SliceSet; the set of age
+ *          `a` lives in slot (head - a) mod ring_len.
+ * For kick k: out_k[i] = factor_k * sum_{a < n_lags_k} conv_a[i] with
+ *   numpy path  (dense=0): conv_a[i] = sum_m m_a[m] * table_k[a][i + S-1 - m],
+ *                          table_k[a] has 2S-1 entries
+ *   dot path    (dense=1): conv_a[i] = sum_j m_a[j] * table_k[a][j][i]
+ * where m_a = moments[slot(a)][source_k].  out_k has the dtype out_dtype. */
+typedef struct phk_wake_kick {
+    int32_t source; /* 0 count, 1 count*mean_x, 2 count*mean_y */
+    int32_t n_lags;
+    int32_t dense;
+    int32_t reserved;
+    double factor;
+    const double *table;
+    void *out;
+} phk_wake_kick;
+
+typedef struct phk_wake_set {
+    int32_t n_slices;
+    int32_t ring_len;
+    int32_t head;
+    int32_t n_kicks;
+    int32_t out_dtype;
+    int32_t reserved;
+    const double *moments;
+    phk_wake_kick kick[PHK_MAX_KICKS];
+} phk_wake_set;
+
+/* ---------------------------------------------------------------------- */
+
+int phk_abi_version(void);
+
+/* Copies the calling thread's last error message (NUL-terminated, at most
+ * len bytes) and returns its full length. */
+int phk_last_error(char *buf, int len);
+
+/* Number of CTAs phk_track() uses for n particles of dtype with an
+ * accumulation over n_slices slices (sizes the partials workspace). */
+int phk_track_grid(int64_t n, int32_t dtype, int32_t n_slices);
+
+/* The fused turn kernel.  In one pass over the particles:
+ *   1. pending (optional): apply the wake kicks left by the previous
+ *      WakeField.track (wake_kicks.py:221-223 and siblings);
+ *   2. program: apply the element sequence (transverse segments with
+ *      chromaticity / amplitude detuning, drifts, RF kicks, linear
+ *      longitudinal maps, transverse shrinking);
+ *   3. acc (optional): bin the updated z and accumulate per-slice count,
+ *      sum x, sum y into acc->partials (and the index array).
+ * Coordinates are written back iff pending or program change them.
+ * Replaces TransverseSegmentMap.track, RFSystems/Drift/Kick/LinearMap.track
+ * and the particle loops of Slicer.slice / mean_per_slice / the kick apply. */
+int phk_track(const phk_program *program, const phk_coords *coords,
+              const phk_kick_set *pending, const phk_accum *acc,
+              void *stream);
+
+/* Merge the per-CTA partials of phk_track in a fixed order into
+ * counts (int32[S]), mean_x / mean_y (double[S], 0 for empty slices:
+ * stats.pyx:251-253) and, if moments_slot != NULL, the wake moment ring
+ * slot double[3][S] = (count, count*mean_x, count*mean_y) as in
+ * wake_kicks.py:217-218.  Any output pointer may be NULL. */
+int phk_slice_finalize(const phk_accum *acc, int32_t *counts, double *mean_x,
+                       double *mean_y, double *moments_slot, void *stream);
+
+/* Wake convolution of every kick of `w` (see phk_wake_set). */
+int phk_wake(const phk_wake_set *w, void *stream);
+
+/* Standalone wake-kick application (when no element program follows). */
+int phk_kick(const phk_coords *coords, const phk_kick_set *kicks, void *stream);
+
+/* Per-slice moments of up to three quantities for Slicer.add_statistics
+ * (slicing.py:443-529, stats.pyx:235-425), two passes:
+ *   pass 0: sums[q][s] += u_q            (q < n_q), counts[s] += 1
+ *   pass 1: sums[3 + pair][s] += (u_a - mean_a[s]) (u_b - mean_b[s])
+ *           for the pairs (0,0) (0,1) (1,1) (0,2) (1,2) (2,2), means given
+ * quantities are device arrays of the coords dtype (n entries); sums is
+ * double[9][S] and counts int32[S], both accumulated (zero them first).  */
+int phk_slice_moments(const phk_slicer *slicer, const void *z, int64_t n,
+                      int32_t dtype, const void *const *quantities, int32_t n_q,
+                      int32_t pass, const double *means, double *sums,
+                      int32_t *counts, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYHEADTAIL_GB300_H */

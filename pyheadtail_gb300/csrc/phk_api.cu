@@ -1,0 +1,272 @@
+// extern "C" entry points of libphk: host-side validation of every
+// argument before any launch, thread-local error messages, dispatch to the
+// launchers in phk_kernels.cu.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "phk_internal.h"
+
+namespace phk {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+const DeviceInfo& device_info() {
+    static std::mutex mu;
+    static std::vector<DeviceInfo> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    for (const DeviceInfo& d : cache)
+        if (d.device == dev) return d;
+    DeviceInfo d;
+    d.device = dev;
+    cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&d.max_smem_optin,
+                           cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (d.sm_count < 1) d.sm_count = 1;
+    if (d.max_smem_optin < 48 * 1024) d.max_smem_optin = 48 * 1024;
+    cache.push_back(d);
+    return cache.back();
+}
+
+static int check_dtype(int32_t dtype, const char* who) {
+    if (dtype != PHK_F64 && dtype != PHK_F32)
+        return set_error(PHK_EPARAM, "%s: unknown dtype %d", who, dtype);
+    return PHK_OK;
+}
+
+static size_t dsize(int32_t dtype) { return dtype == PHK_F64 ? 8 : 4; }
+
+static int check_slicer(const phk_slicer* s, const char* who) {
+    if (!s->edges) return set_error(PHK_ENULL, "%s: slicer edges is NULL", who);
+    if (s->n_slices < 1 || s->n_slices > PHK_MAX_SLICES)
+        return set_error(PHK_ESIZE, "%s: n_slices %d outside [1, %d]", who,
+                         s->n_slices, PHK_MAX_SLICES);
+    if (s->negate != 0 && s->negate != 1)
+        return set_error(PHK_EPARAM, "%s: negate must be 0 or 1", who);
+    return PHK_OK;
+}
+
+static int check_coords(const phk_coords* c, const char* who) {
+    if (!c) return set_error(PHK_ENULL, "%s: coords is NULL", who);
+    int r = check_dtype(c->dtype, who);
+    if (r) return r;
+    if (c->n < 0) return set_error(PHK_ESIZE, "%s: n = %lld < 0", who,
+                                   (long long)c->n);
+    const void* p[6] = {c->x, c->xp, c->y, c->yp, c->z, c->dp};
+    const size_t al = dsize(c->dtype);
+    for (int q = 0; q < 6; ++q) {
+        if (c->n > 0 && !p[q])
+            return set_error(PHK_ENULL, "%s: coordinate %d is NULL", who, q);
+        if (reinterpret_cast<uintptr_t>(p[q]) % al)
+            return set_error(PHK_EALIGN, "%s: coordinate %d not %zu-byte "
+                             "aligned", who, q, al);
+    }
+    return PHK_OK;
+}
+
+static int check_program(const phk_program* p, const char* who) {
+    if (!p) return set_error(PHK_ENULL, "%s: program is NULL", who);
+    if (p->n_ops < 0 || p->n_ops > PHK_MAX_OPS)
+        return set_error(PHK_ESIZE, "%s: n_ops %d outside [0, %d]", who,
+                         p->n_ops, PHK_MAX_OPS);
+    if (p->n_det < 0 || p->n_det > PHK_MAX_DETUNERS)
+        return set_error(PHK_ESIZE, "%s: n_det %d outside [0, %d]", who,
+                         p->n_det, PHK_MAX_DETUNERS);
+    for (int o = 0; o < p->n_ops; ++o) {
+        const phk_op& op = p->op[o];
+        if (op.kind < PHK_OP_TRANSVERSE || op.kind > PHK_OP_SCALE_TRANS)
+            return set_error(PHK_EPARAM, "%s: op %d has unknown kind %d", who,
+                             o, op.kind);
+        if (op.kind == PHK_OP_TRANSVERSE && (op.flags & PHK_FLAG_DETUNED)) {
+            if (op.det_begin < 0 || op.det_count < 0 ||
+                op.det_begin + op.det_count > p->n_det)
+                return set_error(PHK_EPARAM, "%s: op %d detuner range "
+                                 "[%d, +%d) outside the %d detuners", who, o,
+                                 op.det_begin, op.det_count, p->n_det);
+        }
+    }
+    for (int d = 0; d < p->n_det; ++d) {
+        const phk_detuner& dt = p->det[d];
+        if (dt.kind == PHK_DET_CHROMA) {
+            if (dt.nx < 1 || dt.nx > PHK_MAX_POLY || dt.ny < 1 ||
+                dt.ny > PHK_MAX_POLY || dt.zx < 0 || dt.zy < 0 ||
+                dt.zx > 4096 || dt.zy > 4096)
+                return set_error(PHK_EPARAM, "%s: detuner %d has a bad "
+                                 "polynomial (nx %d ny %d zx %d zy %d)", who,
+                                 d, dt.nx, dt.ny, dt.zx, dt.zy);
+        } else if (dt.kind != PHK_DET_AMPLITUDE) {
+            return set_error(PHK_EPARAM, "%s: detuner %d has unknown kind %d",
+                             who, d, dt.kind);
+        }
+    }
+    return PHK_OK;
+}
+
+static int check_kicks(const phk_kick_set* k, int32_t dtype, const char* who) {
+    int r = check_slicer(&k->slicer, who);
+    if (r) return r;
+    if (k->n_kicks < 0 || k->n_kicks > PHK_MAX_KICKS)
+        return set_error(PHK_ESIZE, "%s: n_kicks %d outside [0, %d]", who,
+                         k->n_kicks, PHK_MAX_KICKS);
+    for (int i = 0; i < k->n_kicks; ++i) {
+        if (!k->kick[i]) return set_error(PHK_ENULL, "%s: kick %d is NULL",
+                                          who, i);
+        if (reinterpret_cast<uintptr_t>(k->kick[i]) % dsize(dtype))
+            return set_error(PHK_EALIGN, "%s: kick %d misaligned", who, i);
+        const int t = k->target[i];
+        if (t != PHK_XP && t != PHK_YP && t != PHK_DP)
+            return set_error(PHK_EPARAM, "%s: kick %d target %d is not xp, "
+                             "yp or dp", who, i, t);
+        const int q = k->quad[i];
+        if (q != -1 && q != PHK_X && q != PHK_Y)
+            return set_error(PHK_EPARAM, "%s: kick %d quad %d is not -1, x "
+                             "or y", who, i, q);
+    }
+    return PHK_OK;
+}
+
+static int check_accum(const phk_accum* a, const char* who) {
+    int r = check_slicer(&a->slicer, who);
+    if (r) return r;
+    if (!a->partials) return set_error(PHK_ENULL, "%s: partials is NULL", who);
+    if (a->grid < 1) return set_error(PHK_ESIZE, "%s: grid %d < 1", who,
+                                      a->grid);
+    const int64_t need = 3LL * a->slicer.n_slices * a->grid;
+    if (a->partials_len < need)
+        return set_error(PHK_EWORKSPACE, "%s: partials hold %lld doubles, "
+                         "%lld needed", who, (long long)a->partials_len,
+                         (long long)need);
+    return PHK_OK;
+}
+
+}  // namespace phk
+
+using namespace phk;
+
+extern "C" {
+
+int phk_abi_version(void) { return PHK_ABI_VERSION; }
+
+int phk_last_error(char* buf, int len) {
+    const int n = (int)strlen(g_err);
+    if (buf && len > 0) {
+        strncpy(buf, g_err, (size_t)len - 1);
+        buf[len - 1] = '\0';
+    }
+    return n;
+}
+
+int phk_track_grid(int64_t n, int32_t dtype, int32_t n_slices) {
+    int r = check_dtype(dtype, "phk_track_grid");
+    if (r) return r;
+    if (n < 0) return set_error(PHK_ESIZE, "phk_track_grid: n < 0");
+    if (n_slices < 1 || n_slices > PHK_MAX_SLICES)
+        return set_error(PHK_ESIZE, "phk_track_grid: n_slices %d outside "
+                         "[1, %d]", n_slices, PHK_MAX_SLICES);
+    return track_grid(n, dtype, n_slices);
+}
+
+int phk_track(const phk_program* program, const phk_coords* coords,
+              const phk_kick_set* pending, const phk_accum* acc,
+              void* stream) {
+    int r = check_program(program, "phk_track");
+    if (r) return r;
+    if ((r = check_coords(coords, "phk_track"))) return r;
+    if (pending && (r = check_kicks(pending, coords->dtype, "phk_track")))
+        return r;
+    if (acc && (r = check_accum(acc, "phk_track"))) return r;
+    if (coords->n == 0 && !acc) return PHK_OK;
+    return launch_track(program, coords, pending, acc, (cudaStream_t)stream);
+}
+
+int phk_slice_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
+                       double* mean_y, double* moments_slot, void* stream) {
+    if (!acc) return set_error(PHK_ENULL, "phk_slice_finalize: acc is NULL");
+    int r = check_accum(acc, "phk_slice_finalize");
+    if (r) return r;
+    return launch_finalize(acc, counts, mean_x, mean_y, moments_slot,
+                           (cudaStream_t)stream);
+}
+
+int phk_wake(const phk_wake_set* w, void* stream) {
+    if (!w) return set_error(PHK_ENULL, "phk_wake: wake set is NULL");
+    if (w->n_slices < 1 || w->n_slices > PHK_MAX_SLICES)
+        return set_error(PHK_ESIZE, "phk_wake: n_slices %d outside [1, %d]",
+                         w->n_slices, PHK_MAX_SLICES);
+    if (w->n_kicks < 0 || w->n_kicks > PHK_MAX_KICKS)
+        return set_error(PHK_ESIZE, "phk_wake: n_kicks %d", w->n_kicks);
+    if (w->ring_len < 1 || w->head < 0 || w->head >= w->ring_len)
+        return set_error(PHK_EPARAM, "phk_wake: ring_len %d head %d",
+                         w->ring_len, w->head);
+    if (!w->moments) return set_error(PHK_ENULL, "phk_wake: moments is NULL");
+    int r = check_dtype(w->out_dtype, "phk_wake");
+    if (r) return r;
+    for (int k = 0; k < w->n_kicks; ++k) {
+        const phk_wake_kick& kk = w->kick[k];
+        if (!kk.table || !kk.out)
+            return set_error(PHK_ENULL, "phk_wake: kick %d table/out NULL", k);
+        if (kk.source < 0 || kk.source > 2)
+            return set_error(PHK_EPARAM, "phk_wake: kick %d source %d", k,
+                             kk.source);
+        if (kk.n_lags < 0 || kk.n_lags > w->ring_len)
+            return set_error(PHK_EPARAM, "phk_wake: kick %d uses %d lags of a "
+                             "%d-slot ring", k, kk.n_lags, w->ring_len);
+        if (kk.dense != 0 && kk.dense != 1)
+            return set_error(PHK_EPARAM, "phk_wake: kick %d dense flag", k);
+    }
+    if (w->n_kicks == 0) return PHK_OK;
+    return launch_wake(w, (cudaStream_t)stream);
+}
+
+int phk_kick(const phk_coords* coords, const phk_kick_set* kicks,
+             void* stream) {
+    int r = check_coords(coords, "phk_kick");
+    if (r) return r;
+    if (!kicks) return set_error(PHK_ENULL, "phk_kick: kicks is NULL");
+    if ((r = check_kicks(kicks, coords->dtype, "phk_kick"))) return r;
+    if (coords->n == 0 || kicks->n_kicks == 0) return PHK_OK;
+    phk_program empty;
+    memset(&empty, 0, sizeof(empty));
+    return launch_track(&empty, coords, kicks, nullptr, (cudaStream_t)stream);
+}
+
+int phk_slice_moments(const phk_slicer* slicer, const void* z, int64_t n,
+                      int32_t dtype, const void* const* quantities,
+                      int32_t n_q, int32_t pass, const double* means,
+                      double* sums, int32_t* counts, void* stream) {
+    const char* who = "phk_slice_moments";
+    if (!slicer) return set_error(PHK_ENULL, "%s: slicer is NULL", who);
+    int r = check_slicer(slicer, who);
+    if (r) return r;
+    if ((r = check_dtype(dtype, who))) return r;
+    if (n < 0) return set_error(PHK_ESIZE, "%s: n < 0", who);
+    if (n_q < 0 || n_q > 3) return set_error(PHK_ESIZE, "%s: n_q %d", who, n_q);
+    if (pass != 0 && pass != 1) return set_error(PHK_EPARAM, "%s: pass", who);
+    if (n > 0 && !z) return set_error(PHK_ENULL, "%s: z is NULL", who);
+    if (!sums) return set_error(PHK_ENULL, "%s: sums is NULL", who);
+    if (pass == 0 && !counts) return set_error(PHK_ENULL, "%s: counts", who);
+    if (pass == 1 && !means) return set_error(PHK_ENULL, "%s: means", who);
+    if (n_q > 0 && !quantities) return set_error(PHK_ENULL, "%s: quantities", who);
+    for (int q = 0; q < n_q; ++q)
+        if (n > 0 && !quantities[q])
+            return set_error(PHK_ENULL, "%s: quantity %d is NULL", who, q);
+    if (n == 0) return PHK_OK;
+    return launch_moments(slicer, z, n, dtype, quantities, n_q, pass, means,
+                          sums, counts, (cudaStream_t)stream);
+}
+
+}  // extern "C"

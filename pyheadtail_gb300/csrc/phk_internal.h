@@ -1,0 +1,38 @@
+// Internal declarations shared by the translation units of libphk.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pyheadtail_gb300.h"
+
+namespace phk {
+
+// thread-local error message, read back by phk_last_error()
+int set_error(int code, const char* fmt, ...);
+
+// device properties of the current device (cached per device)
+struct DeviceInfo {
+    int device;
+    int sm_count;
+    int max_smem_optin;
+};
+const DeviceInfo& device_info();
+
+constexpr int kTrackThreads = 256;
+
+// launchers (phk_kernels.cu); arguments already validated by phk_api.cu
+int launch_track(const phk_program* prog, const phk_coords* c,
+                 const phk_kick_set* pk, const phk_accum* acc,
+                 cudaStream_t stream);
+int track_grid(int64_t n, int32_t dtype, int32_t n_slices);
+size_t track_smem_bytes(int32_t dtype, int32_t acc_slices, int32_t pk_slices);
+int launch_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
+                    double* mean_y, double* moments, cudaStream_t stream);
+int launch_wake(const phk_wake_set* w, cudaStream_t stream);
+int launch_moments(const phk_slicer* s, const void* z, int64_t n,
+                   int32_t dtype, const void* const* q, int32_t n_q,
+                   int32_t pass, const double* means, double* sums,
+                   int32_t* counts, cudaStream_t stream);
+
+}  // namespace phk

@@ -1,0 +1,303 @@
+"""Particles with device-resident SoA coordinates.
+
+Mirrors PyHEADTAIL's ``Particles`` (particles/particles.py:16-390): the same
+constructor, the gamma / beta / betagamma / p0 property chain evaluated on
+the host with the same NumPy formulas (so the scalars follow the
+reference bit for bit, including the p0 setter round trip of
+:99-104), SliceSet caching keyed by the slicer (:118-147, :210-215) and
+the bunch statistics (:311-390).
+
+The six coordinates ``x, xp, y, yp, z, dp`` are torch CUDA tensors of one
+dtype: float64 (``precision='fp64'``, the plain drop-in form) or float32
+(``precision='fp32'``, the precision form).  Elements of this package do
+not touch them directly; they append ops to the beam's pending program
+(see ``pyheadtail_gb300._engine``), which runs as one fused kernel when a
+coordinate, a slice set or a statistic is needed.  Reading ``beam.x``
+therefore always returns the current state.
+"""
+import numpy as np
+import torch
+from scipy.constants import c, e
+
+from .. import _engine as E
+from .. import _native as N
+from ..general.element import Printing
+
+COORDS = ('x', 'xp', 'y', 'yp', 'z', 'dp')
+
+
+def _as_tensor(array, dtype, device):
+    if isinstance(array, torch.Tensor):
+        t = array.detach().to(device=device, dtype=dtype)
+        return t.clone().contiguous() if t.data_ptr() == array.data_ptr() \
+            else t.contiguous()
+    return torch.as_tensor(np.ascontiguousarray(array), dtype=dtype,
+                           device=device).contiguous()
+
+
+class Particles(Printing):
+    """Beam of macroparticles; see module docstring.
+
+    Extra keyword arguments beyond the reference's: ``precision`` ('fp64'
+    or 'fp32') and ``device`` (a CUDA device, default the current one).
+    """
+
+    def __init__(self, macroparticlenumber, particlenumber_per_mp, charge,
+                 mass, circumference, gamma, coords_n_momenta_dict={},
+                 *args, **kwargs):
+        precision = kwargs.get('precision', 'fp64')
+        if precision not in ('fp64', 'fp32'):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        if not torch.cuda.is_available():
+            raise N.PhkError('pyheadtail_gb300.Particles needs a CUDA device '
+                             '(sm_103a); there is no CPU path')
+        N.load()
+        self.precision = precision
+        self._code = N.PHK_F64 if precision == 'fp64' else N.PHK_F32
+        self._dtype = E.torch_dtype(self._code)
+        self._device = torch.device(kwargs.get('device', 'cuda'))
+        self._c = {}
+        self._engine = E.Engine(self)
+        self.macroparticlenumber = int(macroparticlenumber)
+        self.particlenumber_per_mp = particlenumber_per_mp
+        self.charge = charge
+        self.mass = mass
+        self.circumference = circumference
+        self.gamma = gamma
+        self._slice_sets = {}
+        self.coords_n_momenta = set()
+        self.id = torch.arange(1, self.macroparticlenumber + 1,
+                               dtype=torch.int32, device=self._device)
+        self.update(coords_n_momenta_dict)
+
+    # -------------------------------------------------- scalar properties
+    @property
+    def intensity(self):
+        return self.particlenumber_per_mp * self.macroparticlenumber
+
+    @intensity.setter
+    def intensity(self, value):
+        self.particlenumber_per_mp = value / float(self.macroparticlenumber)
+
+    @property
+    def charge_per_mp(self):
+        return self.particlenumber_per_mp * self.charge
+
+    @charge_per_mp.setter
+    def charge_per_mp(self, value):
+        self.particlenumber_per_mp = value / self.charge
+
+    @property
+    def gamma(self):
+        return self._gamma
+
+    @gamma.setter
+    def gamma(self, value):
+        self._gamma = value
+        self._beta = np.sqrt(1 - self.gamma**-2)
+        self._betagamma = np.sqrt(self.gamma**2 - 1)
+        self._p0 = self.betagamma * self.mass * c
+
+    @property
+    def beta(self):
+        return self._beta
+
+    @beta.setter
+    def beta(self, value):
+        self.gamma = 1. / np.sqrt(1 - value**2)
+
+    @property
+    def betagamma(self):
+        return self._betagamma
+
+    @betagamma.setter
+    def betagamma(self, value):
+        self.gamma = np.sqrt(value**2 + 1)
+
+    @property
+    def p0(self):
+        return self._p0
+
+    @p0.setter
+    def p0(self, value):
+        self.gamma = np.sqrt(1 + (value / (self.mass * c))**2)
+
+    # -------------------------------------------------- coordinates
+    def _get(self, name):
+        if name not in self._c:
+            raise AttributeError(name)
+        self._engine.sync_for(name)
+        return self._c[name]
+
+    def _set(self, name, value):
+        if name in self._c and value is self._c[name]:
+            return
+        self._engine.flush()
+        self._engine.z_version += 1
+        t = _as_tensor(value, self._dtype, self._device)
+        if t.shape != (self.macroparticlenumber,):
+            raise ValueError('lengths of given phase space coordinate arrays '
+                             'do not coincide with self.macroparticlenumber.')
+        self._c[name] = t
+
+    x = property(lambda s: s._get('x'), lambda s, v: s._set('x', v))
+    xp = property(lambda s: s._get('xp'), lambda s, v: s._set('xp', v))
+    y = property(lambda s: s._get('y'), lambda s, v: s._set('y', v))
+    yp = property(lambda s: s._get('yp'), lambda s, v: s._set('yp', v))
+    z = property(lambda s: s._get('z'), lambda s, v: s._set('z', v))
+    dp = property(lambda s: s._get('dp'), lambda s, v: s._set('dp', v))
+
+    @property
+    def z_beamframe(self):
+        return self.z * self.gamma
+
+    @z_beamframe.setter
+    def z_beamframe(self, value):
+        self.z = value / self.gamma
+
+    def get_coords_n_momenta_dict(self):
+        return {k: getattr(self, k) for k in self.coords_n_momenta}
+
+    def update(self, coords_n_momenta_dict):
+        """particles/particles.py:217-229 (copies the arrays to the device)."""
+        if any(len(v) != self.macroparticlenumber
+               for v in coords_n_momenta_dict.values()):
+            raise ValueError('lengths of given phase space coordinate arrays '
+                             'do not coincide with self.macroparticlenumber.')
+        for k, v in coords_n_momenta_dict.items():
+            if k in COORDS:
+                self._set(k, v)
+            else:
+                setattr(self, k, _as_tensor(v, self._dtype, self._device))
+        self.coords_n_momenta.update(coords_n_momenta_dict.keys())
+
+    def add(self, coords_n_momenta_dict):
+        if any(s in self.coords_n_momenta for s in coords_n_momenta_dict):
+            raise ValueError('One or more of the specified coordinates or '
+                             'momenta already exist and cannot be added. Use '
+                             'self.update(...) for this purpose.')
+        self.update(coords_n_momenta_dict)
+
+    def coords_numpy(self):
+        """float64 NumPy copies of the six coordinates (synchronises)."""
+        return {k: getattr(self, k).double().cpu().numpy() for k in COORDS
+                if k in self._c}
+
+    def sort_for(self, attr):
+        self.reorder(torch.argsort(getattr(self, attr)))
+
+    def reorder(self, permutation, except_for_attrs=[]):
+        self._engine.flush()
+        for attr in ['id'] + list(self.coords_n_momenta):
+            if attr in except_for_attrs:
+                continue
+            if attr in COORDS:
+                self._c[attr] = self._c[attr][permutation].contiguous()
+            else:
+                setattr(self, attr, getattr(self, attr)[permutation])
+        self.clean_slices()
+
+    # -------------------------------------------------- slicing
+    def get_slices(self, slicer, *args, **kwargs):
+        """particles/particles.py:118-147."""
+        if slicer not in self._slice_sets or kwargs.get('statistics'):
+            self._slice_sets[slicer] = slicer.slice(self, *args, **kwargs)
+        return self._slice_sets[slicer]
+
+    def clean_slices(self):
+        self._slice_sets = {}
+
+    # -------------------------------------------------- statistics
+    def _mean(self, name):
+        return float(torch.mean(getattr(self, name).double()))
+
+    def mean_x(self, **kwargs):
+        return self._mean('x')
+
+    def mean_xp(self, **kwargs):
+        return self._mean('xp')
+
+    def mean_y(self, **kwargs):
+        return self._mean('y')
+
+    def mean_yp(self, **kwargs):
+        return self._mean('yp')
+
+    def mean_z(self, **kwargs):
+        return self._mean('z')
+
+    def mean_dp(self, **kwargs):
+        return self._mean('dp')
+
+    def _cov(self, a, b):
+        """Covariance with n-1 normalisation (cobra_functions/stats.pyx:17-45,
+        evaluated as a two-pass sum on the device)."""
+        a = getattr(self, a).double()
+        b = getattr(self, b).double()
+        n = a.numel()
+        if n < 2:
+            return 0.
+        return float(torch.sum((a - a.mean()) * (b - b.mean())) / (n - 1))
+
+    def sigma_x(self, **kwargs):
+        return np.sqrt(self._cov('x', 'x'))
+
+    def sigma_y(self, **kwargs):
+        return np.sqrt(self._cov('y', 'y'))
+
+    def sigma_z(self, **kwargs):
+        return np.sqrt(self._cov('z', 'z'))
+
+    def sigma_xp(self, **kwargs):
+        return np.sqrt(self._cov('xp', 'xp'))
+
+    def sigma_yp(self, **kwargs):
+        return np.sqrt(self._cov('yp', 'yp'))
+
+    def sigma_dp(self, **kwargs):
+        return np.sqrt(self._cov('dp', 'dp'))
+
+    def _emittance(self, u, up, dp):
+        """stats.pyx:83-122."""
+        cu2 = self._cov(u, u)
+        cup2 = self._cov(up, up)
+        cuup = self._cov(up, u)
+        t11 = t12 = t22 = 0.
+        if dp is not None:
+            cdp2 = self._cov(dp, dp)
+            if cdp2 != 0:
+                cudp = self._cov(u, dp)
+                cupdp = self._cov(up, dp)
+                t11 = cudp * cudp / cdp2
+                t12 = cudp * cupdp / cdp2
+                t22 = cupdp * cupdp / cdp2
+        s11, s12, s22 = cu2 - t11, cuup - t12, cup2 - t22
+        return np.sqrt(s11 * s22 - s12 * s12)
+
+    def effective_normalized_emittance_x(self, **kwargs):
+        return self._emittance('x', 'xp', None) * self.betagamma
+
+    def effective_normalized_emittance_y(self, **kwargs):
+        return self._emittance('y', 'yp', None) * self.betagamma
+
+    def effective_normalized_emittance_z(self, **kwargs):
+        return 4 * np.pi * self._emittance('z', 'dp', None) * self.p0 / e
+
+    def epsn_x(self, **kwargs):
+        return self._emittance('x', 'xp', 'dp') * self.betagamma
+
+    def epsn_y(self, **kwargs):
+        return self._emittance('y', 'yp', 'dp') * self.betagamma
+
+    def epsn_z(self, **kwargs):
+        return self.effective_normalized_emittance_z(**kwargs)
+
+    def dispersion_x(self):
+        x, dp = self.x.double(), self.dp.double()
+        d2 = float(torch.mean(dp * dp))
+        return float(torch.mean(x * dp)) / d2 if d2 > 0 else 0
+
+    def dispersion_y(self):
+        y, dp = self.y.double(), self.dp.double()
+        d2 = float(torch.mean(dp * dp))
+        return float(torch.mean(y * dp)) / d2 if d2 > 0 else 0

@@ -1,0 +1,125 @@
+"""CPU checks of the native boundary and of the host logic (no GPU calls).
+
+* libphk.so builds for sm_103a, loads, and exports every entry point that
+  include/pyheadtail_gb300.h declares;
+* the ctypes structures have the C layout (sizes and offsets);
+* the exact slice-edge tables reproduce int32(floor((z - tail)/width)) for
+  every z, in FP64 and for FP32 coordinates, for both signs of the width.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, 'include', 'pyheadtail_gb300.h')
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+    return sorted(set(re.findall(r'\bint\s+(phk_\w+)\s*\(', src)))
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from pyheadtail_gb300 import _build
+    path = _build.build()
+    return ctypes.CDLL(path)
+
+
+def test_library_exports_every_declared_entry_point(lib):
+    names = declared_functions()
+    assert len(names) >= 8
+    for n in names:
+        assert hasattr(lib, n), n
+    from pyheadtail_gb300 import _native
+    assert set(names) <= set(_native.SIGNATURES)
+
+
+def test_abi_version(lib):
+    lib.phk_abi_version.restype = ctypes.c_int
+    assert lib.phk_abi_version() == 1
+
+
+def test_host_validation_without_gpu(lib):
+    """Argument errors are caught on the host before any CUDA call."""
+    from pyheadtail_gb300 import _native as N
+    L = N.load(build_if_missing=False)
+    prog = N.Program()
+    prog.n_ops = 99
+    coords = N.Coords()
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(coords), None, None,
+                       None) == -2
+    assert 'n_ops' in N.last_error()
+    prog.n_ops = 0
+    coords.n = -5
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(coords), None, None,
+                       None) == -2
+    coords.n = 10
+    coords.dtype = 7
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(coords), None, None,
+                       None) == -4
+    coords.dtype = 0
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(coords), None, None,
+                       None) == -1          # NULL coordinate pointers
+    for i, f in enumerate(('x', 'xp', 'y', 'yp', 'z', 'dp')):
+        setattr(coords, f, 4096 * (i + 1) + 4)   # 4-byte aligned only
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(coords), None, None,
+                       None) == -3
+    ws = N.WakeSet()
+    ws.n_slices = 0
+    assert L.phk_wake(ctypes.byref(ws), None) == -2
+    acc = N.Accum()
+    acc.slicer.n_slices = 10
+    acc.slicer.edges = 4096
+    acc.partials = 8192
+    acc.grid = 4
+    acc.partials_len = 100
+    for i, f in enumerate(('x', 'xp', 'y', 'yp', 'z', 'dp')):
+        setattr(coords, f, 4096 * (i + 1))
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(coords), None,
+                       ctypes.byref(acc), None) == -6
+    assert 'partials' in N.last_error()
+
+
+def test_struct_layout_matches_header():
+    from pyheadtail_gb300 import _native as N
+    assert ctypes.sizeof(N.Coords) == 64
+    assert ctypes.sizeof(N.Slicer) == 48
+    assert ctypes.sizeof(N.Op) == 24 + 24 * 8
+    assert ctypes.sizeof(N.Detuner) == 24 + 16 * 8
+    assert ctypes.sizeof(N.Program) == 8 + 12 * 216 + 6 * 152
+    assert N.KickSet.kick.offset == 120
+    assert ctypes.sizeof(N.KickSet) == 184
+    assert ctypes.sizeof(N.Accum) == 80
+    assert ctypes.sizeof(N.WakeKick) == 40
+    assert N.WakeSet.kick.offset == 32
+
+
+@pytest.mark.parametrize('code', [0, 1])
+@pytest.mark.parametrize('cuts,S', [((-0.69, 0.69), 50), ((-0.31, 0.05), 7),
+                                    ((0.2, -0.2), 13), ((-3e-3, 1e-2), 500),
+                                    ((-1.1, 1.3), 1000)])
+def test_exact_edges_reproduce_reference_index(code, cuts, S):
+    from pyheadtail_gb300 import _engine as E
+    tail, head = cuts
+    width = (head - tail) / float(S)
+    e, neg = E.exact_edges(tail, width, S, code)
+    dt = np.float64 if code == 0 else np.float32
+    rng = np.random.RandomState(S)
+    span = abs(head - tail)
+    z = (rng.uniform(min(tail, head) - 0.1 * span, max(tail, head) +
+                     0.1 * span, 200000)).astype(dt)
+    # add every edge and its neighbours
+    ez = (-e if neg else e).astype(dt)
+    z = np.concatenate([z, ez, np.nextafter(ez, dt(np.inf)),
+                        np.nextafter(ez, dt(-np.inf))])
+    want = np.floor((z.astype(np.float64) - tail) / width)
+    u = -z if neg else z
+    inside = (u >= e[0]) & (u < e[-1])
+    got = np.searchsorted(e, u, side='right') - 1
+    assert np.array_equal(inside, (want >= 0) & (want < S))
+    assert np.array_equal(got[inside], want[inside].astype(np.int64))

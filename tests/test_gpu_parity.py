@@ -1,0 +1,227 @@
+"""Parity of the plain FP64 GPU path with the reference.
+
+* every golden fixture (made by running PyHEADTAIL itself) is replayed on
+  the GPU from the same initial coordinates: slice indices, counts and beam
+  scalars bit-exact, coordinates and slice means within 1e-12 relative to
+  the coordinate's RMS;
+* the C1 workload at its full size (1e5 macroparticles, 100 turns) and the
+  C2 / multi-turn workloads at reduced size are compared with the oracle
+  (the oracle is bit-identical to the reference on the fixtures);
+* at full workload sizes, the GPU slice index of every particle is checked
+  bit for bit against the reference formula evaluated by torch on the GPU
+  coordinates.
+"""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip('torch')
+
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, '*.npz')))
+COORDS = ('x', 'xp', 'y', 'yp', 'z', 'dp')
+RTOL = 1e-12        # coordinates / slice means, relative to the RMS
+
+
+def rms_err(got, ref):
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = np.sqrt(np.mean(ref**2)) if ref.size else 1.
+    if scale == 0:
+        scale = 1.
+    return float(np.max(np.abs(got - ref)) / scale) if ref.size else 0.
+
+
+def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9):
+    for k, v in ref.items():
+        if not k.startswith('t'):
+            continue
+        assert k in rec, '%s: missing %s' % (label, k)
+        g = rec[k]
+        if k.endswith(('_idx', '_counts', '_gamma', '_p0', '_z_bins')):
+            np.testing.assert_array_equal(np.asarray(g), v,
+                                          err_msg='%s %s' % (label, k))
+        elif k.endswith(('_mean_x', '_mean_y')) and np.ndim(v) == 0:
+            assert abs(g - v) <= 1e-12 * max(abs(v), 1e-30) + 1e-18, (label, k)
+        elif any(k.endswith('_' + c) for c in COORDS) and np.ndim(v) == 1 \
+                and len(k.split('_')) == 2:
+            e = rms_err(g, v)
+            assert e <= rtol, '%s %s: rel err %.3g' % (label, k, e)
+        else:
+            # per-slice statistics: skip slices where the reference itself
+            # is not finite (sqrt of a negative determinant)
+            v = np.asarray(v, dtype=np.float64)
+            g = np.asarray(g, dtype=np.float64)
+            ok = np.isfinite(v)
+            tol = rtol if 'mean' in k else stat_rtol
+            e = rms_err(g[ok], v[ok])
+            assert e <= tol, '%s %s: rel err %.3g' % (label, k, e)
+
+
+def load(path):
+    with np.load(path) as f:
+        return {k: f[k] for k in f.files}
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from pyheadtail_gb300 import _native
+    return _native.load()
+
+
+@pytest.mark.parametrize('path', FIXTURES,
+                         ids=[os.path.basename(p)[:-4] for p in FIXTURES])
+def test_golden_fixture_fp64(lib, path):
+    import gpu_cases as G
+    ref = load(path)
+    spec = json.loads(str(ref['spec']))
+    coords = {k: ref['init_' + k] for k in COORDS}
+    beam = G.make_beam(spec['beam'], coords)
+    rec = G.run(spec, beam)
+    compare(rec, ref, os.path.basename(path))
+
+
+def _oracle_vs_gpu(spec, n_turns, record_turns=None):
+    import gpu_cases as G
+    from oracle import cases as OC
+    obeam = OC.make_beam(spec['beam'])
+    coords = obeam.coords()
+    ref = OC.run(spec, obeam, n_turns=n_turns, record_turns=record_turns)
+    beam = G.make_beam(spec['beam'], coords)
+    rec = G.run(spec, beam, n_turns=n_turns, record_turns=record_turns)
+    return rec, ref
+
+
+def test_c1_full_size_100_turns(lib):
+    """C1: 1e5 macroparticles, seed 0, linear maps, 50 slices, resonator."""
+    import cases as C
+    spec = dict(C.CASES['c1_full'])
+    spec['beam'] = C.beam_params(100000, 0)
+    rec, ref = _oracle_vs_gpu(spec, 100)
+    compare(rec, ref, 'c1 100 turns')
+
+
+def test_c2_reduced_size(lib):
+    """C2 physics (Q'=5, amplitude detuning, h=4620 RF, 200 slices,
+    resonator) at 1e5 macroparticles, 30 turns."""
+    import cases as C
+    spec = dict(C.CASES['c2_full'])
+    spec['beam'] = C.beam_params(100000, 1)
+    rec, ref = _oracle_vs_gpu(spec, 30)
+    compare(rec, ref, 'c2 30 turns')
+
+
+def test_multiturn_wake_reduced_size(lib):
+    """C3 wake model (500 slices, resonator + 50-turn resistive wall) at
+    2e4 macroparticles over 60 turns (history full after 50)."""
+    import cases as C
+    spec = dict(beam=C.beam_params(20000, 2), n_turns=60, elements=[
+        C.smooth_transverse(), C.rf(),
+        C.wake(C.slicer(500), C.resonator(),
+               C.resistive_wall(n_turns_wake=50))])
+    rec, ref = _oracle_vs_gpu(spec, 60, record_turns=(0, 49, 59))
+    compare(rec, ref, 'multiturn 60 turns')
+
+
+@pytest.mark.parametrize('n', [1, 2, 3, 5, 1001, 4099])
+def test_ragged_sizes(lib, n):
+    """Sizes that are not multiples of the vector width or of a tile."""
+    import cases as C
+    spec = dict(C.CASES['c2_full'])
+    spec['beam'] = C.beam_params(n, 5)
+    rec, ref = _oracle_vs_gpu(spec, 3)
+    compare(rec, ref, 'n=%d' % n)
+
+
+def test_edges_outside_nan_and_misaligned(lib):
+    """Particles exactly on bin edges, just below them, outside the cuts,
+    NaN z, and coordinate tensors that are views at an odd offset (not
+    16-byte aligned: scalar path)."""
+    import gpu_cases as G
+    from oracle import turn_loop as T
+    from pyheadtail_gb300 import _engine as E
+    import cases as C
+    bp = C.beam_params(4000, 7)
+    rng = np.random.RandomState(3)
+    S, cuts = 40, (-0.69, 0.69)
+    width = (cuts[1] - cuts[0]) / float(S)
+    edges, _ = E.exact_edges(cuts[0], width, S, E._F64)
+    z = rng.normal(0, 0.4, 4000)
+    z[:41] = edges
+    z[41:82] = np.nextafter(edges, -np.inf)
+    z[82] = np.nan
+    z[83:90] = [-5., 5., 0.69, -0.69, 1e300, -1e300, 0.]
+    coords = dict(x=rng.normal(0, 1e-3, 4000), xp=rng.normal(0, 1e-5, 4000),
+                  y=rng.normal(0, 1e-3, 4000), yp=rng.normal(0, 1e-5, 4000),
+                  z=z, dp=rng.normal(0, 1e-3, 4000))
+    beam = G.make_beam(bp, coords)
+    # re-seat every coordinate as a view one element into a larger buffer
+    for k in COORDS:
+        big = torch.empty(4001, dtype=torch.float64, device='cuda')
+        big[1:] = beam._c[k]
+        beam._c[k] = big[1:]
+    sl = G.make_slicer(C.slicer(S, z_cuts=cuts))
+    ss = sl.slice(beam, statistics=['mean_x', 'mean_y'])
+    idx = ss.slice_index_of_particle.cpu().numpy()
+    with np.errstate(invalid='ignore'):
+        want = np.floor((z - cuts[0]) / width)
+    want_i = np.where(np.isfinite(want) & (np.abs(want) < 2**31), want,
+                      -2**31).astype(np.int64)
+    np.testing.assert_array_equal(idx.astype(np.int64), want_i)
+    ob = T.Beam(coords, 1., 1., 1., 1., 27.7)
+    oss = T.UniformBinSlicer(S, z_cuts=cuts).slice(ob, ['mean_x', 'mean_y'])
+    np.testing.assert_array_equal(ss.n_macroparticles_per_slice.cpu().numpy(),
+                                  oss.n_macroparticles_per_slice)
+    assert rms_err(ss.mean_x.cpu().numpy(), oss.mean_x) <= RTOL
+
+
+def test_all_outside_and_empty_slices(lib):
+    import gpu_cases as G
+    import cases as C
+    n = 777
+    coords = {k: np.zeros(n) for k in COORDS}
+    coords['z'] = np.full(n, 3.0)
+    beam = G.make_beam(C.beam_params(n, 1), coords)
+    sl = G.make_slicer(C.slicer(20))
+    ss = sl.slice(beam, statistics=['mean_x', 'mean_y'])
+    assert int(ss.n_macroparticles_per_slice.sum()) == 0
+    assert float(ss.mean_x.abs().sum()) == 0.0
+    assert int((ss.slice_index_of_particle >= 0).sum()) == n   # 5 * 20 / 1.38
+
+
+@pytest.mark.parametrize('n,S', [(10**7, 500), (5 * 10**7, 1000)])
+def test_full_size_binning_bit_exact(lib, n, S):
+    """C3 / C5 sizes: every particle's slice index equals the reference
+    formula int32(floor((z - tail)/width)) evaluated by torch in FP64."""
+    import gpu_cases as G
+    import cases as C
+    from pyheadtail_gb300.particles.generators import \
+        gaussian_bunch_coordinates
+    torch.manual_seed(0)
+    z = torch.randn(n, dtype=torch.float64, device='cuda') * 0.23
+    coords = {k: torch.zeros(n, dtype=torch.float64, device='cuda')
+              for k in COORDS}
+    coords['z'] = z
+    coords['x'] = torch.randn(n, dtype=torch.float64, device='cuda') * 1e-3
+    beam = G.make_beam(C.beam_params(n, 2), coords)
+    sl = G.make_slicer(C.slicer(S))
+    ss = sl.slice(beam, statistics=['mean_x', 'mean_y'])
+    idx = ss.slice_index_of_particle
+    tail, head = C.Z_CUTS
+    width = (head - tail) / float(S)
+    want = torch.floor((beam.z - tail) / width).to(torch.int32)
+    assert torch.equal(idx, want)
+    inside = (want >= 0) & (want < S)
+    counts = torch.bincount(want[inside].long(), minlength=S).to(torch.int32)
+    assert torch.equal(ss.n_macroparticles_per_slice, counts)
+    sums = torch.zeros(S, dtype=torch.float64, device='cuda')
+    sums.index_add_(0, want[inside].long(), beam.x[inside])
+    mean = torch.where(counts > 0, sums / counts.clamp(min=1).double(),
+                       torch.zeros_like(sums))
+    assert float((mean - ss.mean_x).abs().max()) <= 1e-12 * float(
+        mean.abs().max())
