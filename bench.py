@@ -1,0 +1,452 @@
+#!/usr/bin/env python
+"""Benchmark of the single-bunch turn loop on one GB300: macroparticle-turns/s.
+
+Default workload (the configuration the headline metric is quoted on):
+  C2 -- 1e6 macroparticles, seed 1, matched 6D Gaussian (eps_n 2.5 um,
+  sigma_z 0.23 m, sigma_dp 1e-3), gamma 27.7, C = 6911.5 m, one transverse
+  segment (Q 20.13 / 20.18, beta 50 m) with Q' = 5 and amplitude detuning
+  (1e-11, 1e-11, -5e-12), RF h = 4620, V = 4.5 MV, UniformBinSlicer 200
+  slices over (-0.69, 0.69) m, broadband resonator (10 MOhm/m, 1 GHz, Q=1).
+A step is one turn: [TransverseSegmentMap, RFSystems, WakeField].
+
+``value``  plain FP64 form (the drop-in), device time of the turn replayed as
+           a CUDA graph, inputs resident, L2 flushed between steps.
+``e2e``    the same turn through the public API (``m.track(beam)`` for each
+           element) with the step's coordinates copied from pinned host memory
+           and the turn's result (bunch centroid) read back, wall clock.
+``forms``  the FP32 precision form measured the same way.
+``--impl reference`` times the CPU oracle (a NumPy restatement of the
+reference's turn loop, bit-identical to it on the golden fixtures) on a
+bounded sample of the same workload on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+C_RING = 6911.5038378975451
+GAMMA = 27.7
+Z_CUTS = (-0.69, 0.69)
+ALPHA_C = 230. * 2 * np.pi * 0.017 / C_RING + GAMMA**-2
+AMP = (1e-11, 1e-11, -5e-12)
+
+WORKLOADS = {
+    'c1': dict(n=100000, seed=0, slices=50, chroma=None, amp=None,
+               longitudinal='linear', rw_turns=0,
+               label='C1: 1e5 mp, linear maps, 50 slices, resonator'),
+    'c2': dict(n=1000000, seed=1, slices=200, chroma=(5., 5.), amp=AMP,
+               longitudinal='rf', rw_turns=0,
+               label="C2: 1e6 mp, Q'=5, amplitude detuning, RF h=4620 "
+                     "V=4.5MV, 200 slices, resonator"),
+    'c3': dict(n=10000000, seed=2, slices=500, chroma=None, amp=None,
+               longitudinal='rf', rw_turns=50,
+               label='C3: 1e7 mp, 500 slices, resonator + 50-turn '
+                     'resistive wall'),
+    'c5': dict(n=50000000, seed=4, slices=1000, chroma=(2., 2.), amp=AMP,
+               longitudinal='rf', rw_turns=50,
+               label="C5: 5e7 mp, Q'=2, amplitude detuning, 1000 slices, "
+                     'resonator + 50-turn resistive wall'),
+}
+
+L2_FLUSH_BYTES = 512 << 20
+
+
+def bunch_coords(w):
+    from pyheadtail_gb300.particles.generators import \
+        gaussian_bunch_coordinates
+    return gaussian_bunch_coordinates(w['n'], w['seed'], GAMMA, 2.5e-6, 2.5e-6,
+                                      50., 50., 0.23, 1e-3)
+
+
+def build_gpu(w, coords, precision):
+    from scipy.constants import e, m_p
+    from pyheadtail_gb300.general.printers import SilentPrinter
+    from pyheadtail_gb300.impedances import wakes as W
+    from pyheadtail_gb300.particles.particles import Particles
+    from pyheadtail_gb300.particles.slicing import UniformBinSlicer
+    from pyheadtail_gb300.trackers.detuners import (AmplitudeDetuning,
+                                                    Chromaticity)
+    from pyheadtail_gb300.trackers.longitudinal_tracking import (LinearMap,
+                                                                 RFSystems)
+    from pyheadtail_gb300.trackers.transverse_tracking import TransverseMap
+    sp = SilentPrinter()
+    beam = Particles(w['n'], 2.5e11 / w['n'], e, m_p, C_RING, GAMMA,
+                     coords_n_momenta_dict=coords, precision=precision)
+    dets = []
+    if w['chroma']:
+        dets.append(Chromaticity(*w['chroma']))
+    if w['amp']:
+        dets.append(AmplitudeDetuning(*w['amp']))
+    z2 = np.zeros(2)
+    tm = TransverseMap(np.array([0., C_RING]), z2, np.array([50., 50.]), z2,
+                       z2, np.array([50., 50.]), z2, 20.13, 20.18, dets,
+                       printer=sp)
+    if w['longitudinal'] == 'rf':
+        lm = RFSystems(C_RING, [4620], [4.5e6], [0.], [ALPHA_C], GAMMA,
+                       charge=e, mass=m_p, printer=sp, warningprinter=sp)
+    else:
+        lm = LinearMap([ALPHA_C], C_RING, 0.017, printer=sp,
+                       warningprinter=sp)
+    sources = [W.CircularResonator(10e6, 1e9, 1.)]
+    if w['rw_turns']:
+        sources.append(W.CircularResistiveWall(0.02, C_RING, 5.8e7, 1e-12,
+                                               n_turns_wake=w['rw_turns']))
+    wf = W.WakeField(UniformBinSlicer(w['slices'], z_cuts=Z_CUTS,
+                                      warningprinter=sp), *sources)
+    return beam, list(tm) + [lm, wf]
+
+
+def build_oracle(w, coords):
+    from scipy.constants import e, m_p
+    from oracle import turn_loop as T
+    n = len(coords['x'])
+    beam = T.Beam(coords, 2.5e11 / n, e, m_p, C_RING, GAMMA)
+    z2 = np.zeros(2)
+    segs = T.transverse_map([0., C_RING], z2, np.array([50., 50.]), z2, z2,
+                            np.array([50., 50.]), z2, 20.13, 20.18,
+                            chroma=w['chroma'], amplitude=w['amp'])
+    if w['longitudinal'] == 'rf':
+        lm = T.RFSystems(C_RING, [4620], [4.5e6], [0.], [ALPHA_C], GAMMA,
+                         charge=e, mass=m_p)
+    else:
+        lm = T.LinearMap([ALPHA_C], C_RING, 0.017)
+    sl = T.UniformBinSlicer(w['slices'], z_cuts=Z_CUTS)
+    kicks = T.circular_resonator_kicks(sl, 10e6, 1e9, 1.)
+    nmax = 1
+    if w['rw_turns']:
+        kicks += T.circular_resistive_wall_kicks(sl, 0.02, C_RING, 5.8e7,
+                                                 1e-12, w['rw_turns'])
+        nmax = w['rw_turns']
+    return beam, list(segs) + [lm, T.WakeField(sl, kicks, nmax)]
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler(object):
+    """nvidia-smi sampling during the timed region (clocks and throttle
+    reasons); never changes any GPU setting."""
+
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,'
+         'clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.dev), '--query-gpu=' + self.Q,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith('active'):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': max(mx),
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def measured_peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per particle of the track kernel from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    p = os.path.join(ROOT, 'profiles', 'traffic.json')
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(kernel_key)
+
+
+def time_form(w, coords, precision, steps, warmup, flush):
+    """Device time per turn (graph replay), track-kernel time, e2e."""
+    import torch
+    from pyheadtail_gb300 import _native as N
+    from pyheadtail_gb300.turngraph import TurnGraph
+    beam, elements = build_gpu(w, coords, precision)
+    ring = max(1, w['rw_turns'])
+    warm = max(warmup, ring + 2, 3)
+    tg = TurnGraph(elements, beam, warmup_turns=warm).capture()
+    tpg = tg.turns_per_graph
+    tg.replay(1)                        # graph warm-up
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    n0 = N.launch_count()
+    for i in range(steps):
+        flush.zero_()                   # evict L2 (outside the timed span)
+        starts[i].record()
+        tg.replay(1)
+        ends[i].record()
+    torch.cuda.synchronize()
+    graph_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    # the graph replays kernels captured through libphk: count them from
+    # one eager turn (same sequence)
+    n_eager0 = N.launch_count()
+    for m in elements:
+        m.track(beam)
+    beam._engine.flush()
+    torch.cuda.synchronize()
+    kernels_per_turn = N.launch_count() - n_eager0
+    del n0
+    # track kernel alone: eager turns with events around phk_track
+    beam._engine.track_events = []
+    for i in range(steps):
+        flush.zero_()
+        for m in elements:
+            m.track(beam)
+    torch.cuda.synchronize()
+    evs = beam._engine.track_events
+    beam._engine.track_events = None
+    track_ms = [a.elapsed_time(b) for a, b in evs]
+    # e2e: public API, inputs from pinned host memory, centroid read back
+    host = {k: torch.from_numpy(np.ascontiguousarray(
+        v.astype(np.float64 if precision == 'fp64' else np.float32))
+    ).pin_memory() for k, v in coords.items()}
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    e2e_s = []
+    for i in range(max(3, steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k, t in host.items():
+            getattr(beam, k).copy_(t, non_blocking=True)
+        for m in elements:
+            m.track(beam)
+        cx, cy = beam.mean_x(), beam.mean_y()
+        e2e_s.append(time.perf_counter() - t0)
+    return dict(graph_ms=graph_ms, turns_per_step=tpg, track_ms=track_ms,
+                e2e_s=e2e_s, h2d=h2d, d2h=16, kernels_per_turn=kernels_per_turn,
+                centroid=(cx, cy))
+
+
+def cpu_baseline(w, coords, budget_s=12.0):
+    """Oracle (NumPy restatement of the reference) on the host, 1 thread,
+    on a bounded sample: full bunch up to 1e6 particles, turns until about
+    budget_s of CPU time."""
+    n = len(coords['x'])
+    ns = min(n, 1000000)
+    sub = {k: v[:ns].copy() for k, v in coords.items()}
+    beam, els = build_oracle(w, sub)
+    for m in els:                       # one untimed turn
+        m.track(beam)
+    t0 = time.perf_counter()
+    turns = 0
+    while True:
+        for m in els:
+            m.track(beam)
+        turns += 1
+        if time.perf_counter() - t0 > budget_s or turns >= 200:
+            break
+    dt = time.perf_counter() - t0
+    return {'value': ns * turns / dt, 'unit': 'macroparticle-turns/s',
+            'cores': 1, 'kind': 'port',
+            'sample': '%d macroparticles x %d turns of the same workload '
+                      '(oracle: NumPy restatement of the reference, single '
+                      'thread, like the reference)' % (ns, turns)}
+
+
+def run_ours(a, rank, world):
+    import torch
+    w = WORKLOADS[a.workload]
+    dev = rank % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
+    coords = bunch_coords(w)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32,
+                        device='cuda')
+    hbm_peak, peak_kind = measured_peaks()
+    sampler = ClockSampler(dev)
+    forms = {}
+    sampler.start()
+    for precision in ('fp64', 'fp32'):
+        if a.form not in ('all', precision):
+            continue
+        r = time_form(w, coords, precision, a.steps, a.warmup, flush)
+        bytes_pp = 96 if precision == 'fp64' else 48
+        step_ms = float(np.sum(r['graph_ms']))
+        turns = a.steps * r['turns_per_step']
+        track_avg = float(np.mean(r['track_ms']))
+        achieved = bytes_pp * w['n'] / (track_avg * 1e-3) / 1e9
+        tpp = profile_traffic('track_%s_%s' % (a.workload, precision))
+        e2e_t = float(np.sum(r['e2e_s']))
+        forms[precision] = {
+            'value': w['n'] * turns / (step_ms * 1e-3),
+            'ms_per_step': step_ms / a.steps,
+            'turns_per_step': r['turns_per_step'],
+            'kernels_per_turn': r['kernels_per_turn'],
+            'roofline': {'bound': 'hbm', 'achieved': achieved,
+                         'peak': hbm_peak, 'unit': 'GB/s',
+                         'frac': achieved / hbm_peak,
+                         'peak_kind': peak_kind,
+                         'traffic': None if tpp is None else tpp * w['n'],
+                         'kernel': 'phk::track_kernel',
+                         'kernel_ms': track_avg,
+                         'algorithmic_bytes_per_launch': bytes_pp * w['n']},
+            'e2e': {'value': w['n'] * len(r['e2e_s']) / e2e_t,
+                    'unit': 'macroparticle-turns/s',
+                    'h2d_bytes_per_step': r['h2d'],
+                    'd2h_bytes_per_step': r['d2h']},
+        }
+    clocks = sampler.stop()
+    # multi-GPU: independent replicas, slowest rank defines the time
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([forms['fp64']['ms_per_step'] if 'fp64' in forms
+                          else forms['fp32']['ms_per_step']], device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    if rank != 0:
+        return
+    head = forms.get('fp64') or forms['fp32']
+    prec = 'fp64' if 'fp64' in forms else 'fp32'
+    out = {
+        'metric': 'macroparticle-turns/s on 1 GB300: FP32/batched vs FP64 '
+                  'plain; % HBM roofline',
+        'value': head['value'] * world,
+        'unit': 'macroparticle-turns/s',
+        'n_gpus': world, 'steps': a.steps, 'warmup': a.warmup,
+        'ms_per_step': head['ms_per_step'],
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64' if prec == 'fp64' else 'f32',
+        'data': 'synthetic: seeded 6D Gaussian bunch (reference generator '
+                'draw order), no dataset',
+        'config': {'workload': w['label'], 'n_macroparticles': w['n'],
+                   'n_slices': w['slices'], 'form': prec,
+                   'turns_per_step': head['turns_per_step'],
+                   'l2': 'flushed between steps (512 MiB write, untimed)',
+                   'timing': 'CUDA events around a CUDA-graph replay of '
+                             'the turn; inputs resident in HBM',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'roofline': head['roofline'],
+        'e2e': head['e2e'],
+        'gpu_launches': head['kernels_per_turn'] * head['turns_per_step'] *
+        a.steps,
+        'clocks': clocks,
+        'forms': forms,
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        out['cpu_baseline'] = cpu_baseline(w, coords)
+    print(json.dumps(out))
+
+
+# ------------------------------------------------------------ reference arm
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    w = WORKLOADS[a.workload]
+    coords = bunch_coords(w)
+    ns = min(w['n'], 200000)
+    sub = {k: v[:ns].copy() for k, v in coords.items()}
+    beam, els = build_oracle(w, sub)
+    for _ in range(a.warmup):
+        for m in els:
+            m.track(beam)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        for m in els:
+            m.track(beam)
+    dt = time.perf_counter() - t0
+    v = ns * a.steps / dt
+    sample = ('%d macroparticles (first %d of the seeded bunch), one turn '
+              'per step' % (ns, ns))
+    print(json.dumps({
+        'impl': 'reference',
+        'metric': 'macroparticle-turns/s on 1 GB300: FP32/batched vs FP64 '
+                  'plain; % HBM roofline',
+        'value': v, 'unit': 'macroparticle-turns/s', 'n_gpus': world,
+        'steps': a.steps, 'warmup': a.warmup,
+        'ms_per_step': dt / a.steps * 1e3, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic: seeded 6D Gaussian bunch',
+        'config': {'workload': w['label'], 'n_macroparticles': w['n'],
+                   'n_slices': w['slices'], 'form': 'fp64'},
+        'cpu_baseline': {'value': v, 'unit': 'macroparticle-turns/s',
+                         'cores': 1, 'kind': 'port', 'sample': sample},
+        'e2e': {'value': v, 'unit': 'macroparticle-turns/s',
+                'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=50)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', choices=['ours', 'reference'], default='ours')
+    ap.add_argument('--workload', choices=sorted(WORKLOADS), default='c2')
+    ap.add_argument('--form', choices=['all', 'fp64', 'fp32'], default='all')
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    a = ap.parse_args()
+    a.warmup = max(3, a.warmup)
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if a.impl == 'reference':
+        return run_reference(a, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', rank)))
+        dist.init_process_group('nccl')
+        dist.barrier()
+    run_ours(a, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

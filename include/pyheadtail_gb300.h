@@ -228,6 +228,10 @@ typedef struct phk_wake_set {
 
 int phk_abi_version(void);
 
+/* Number of kernels the library has launched in this process (all
+ * devices, all threads): lets a caller verify which work ran natively. */
+int64_t phk_launch_count(void);
+
 /* Copies the calling thread's last error message (NUL-terminated, at most
  * len bytes) and returns its full length. */
 int phk_last_error(char *buf, int len);

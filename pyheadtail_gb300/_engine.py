@@ -249,6 +249,9 @@ class Engine(object):
         self._workspaces = {}
         self.launches = 0
         self.z_version = 0     # bumped whenever z may have changed
+        # optional list; when set, (start, end) CUDA events are recorded
+        # around every fused track launch (used to time the kernel alone)
+        self.track_events = None
 
     # -- building
     def enqueue(self, op):
@@ -311,9 +314,17 @@ class Engine(object):
         coords = self.coords_struct()
         ks = self.kick.struct() if self.kick is not None else None
         ac = acc.struct() if acc is not None else None
+        ev = None
+        if self.track_events is not None:
+            ev = (torch.cuda.Event(enable_timing=True),
+                  torch.cuda.Event(enable_timing=True))
+            ev[0].record()
         N.call('phk_track', ctypes.byref(prog), ctypes.byref(coords),
                ctypes.byref(ks) if ks is not None else None,
                ctypes.byref(ac) if ac is not None else None, stream_handle())
+        if ev is not None:
+            ev[1].record()
+            self.track_events.append(ev)
         self.launches += 1
         if self.ops:
             self.z_version += 1

@@ -98,6 +98,7 @@ class PhkError(RuntimeError):
 # name -> (argtypes); every entry point returns int
 SIGNATURES = {
     'phk_abi_version': [],
+    'phk_launch_count': [],
     'phk_last_error': [ctypes.c_char_p, ctypes.c_int],
     'phk_track_grid': [ctypes.c_int64, ctypes.c_int32, ctypes.c_int32],
     'phk_track': [ctypes.POINTER(Program), ctypes.POINTER(Coords),
@@ -139,11 +140,17 @@ def load(build_if_missing=True):
     for name, argtypes in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.argtypes = argtypes
-        fn.restype = ctypes.c_int
+        fn.restype = ctypes.c_int64 if name == 'phk_launch_count' \
+            else ctypes.c_int
     if lib.phk_abi_version() != 1:
         raise PhkError('libphk ABI version mismatch')
     _lib = lib
     return lib
+
+
+def launch_count():
+    """Kernels launched by libphk in this process so far."""
+    return int(load().phk_launch_count())
 
 
 def last_error():
@@ -159,5 +166,12 @@ def check(status, what):
     return status
 
 
+# observers of native calls (pyheadtail_gb300.turngraph records the
+# parameters of a turn to verify that it is stationary)
+RECORDERS = []
+
+
 def call(name, *args):
+    for r in RECORDERS:
+        r(name, args)
     return check(getattr(load(), name)(*args), name)

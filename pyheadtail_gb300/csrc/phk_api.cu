@@ -6,6 +6,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -14,6 +15,9 @@
 namespace phk {
 
 static thread_local char g_err[512] = "";
+static std::atomic<int64_t> g_launches(0);
+
+void count_launches(int n) { g_launches.fetch_add(n); }
 
 int set_error(int code, const char* fmt, ...) {
     va_list ap;
@@ -160,6 +164,8 @@ using namespace phk;
 extern "C" {
 
 int phk_abi_version(void) { return PHK_ABI_VERSION; }
+
+int64_t phk_launch_count(void) { return g_launches.load(); }
 
 int phk_last_error(char* buf, int len) {
     const int n = (int)strlen(g_err);

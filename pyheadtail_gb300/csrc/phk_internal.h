@@ -8,6 +8,9 @@
 
 namespace phk {
 
+// kernels launched by the library (phk_launch_count)
+void count_launches(int n);
+
 // thread-local error message, read back by phk_last_error()
 int set_error(int code, const char* fmt, ...);
 

@@ -487,12 +487,24 @@ size_t track_smem_bytes(int32_t dtype, int32_t Sa, int32_t Sp) {
                             : smem_bytes<float, 4>(Sa, Sp);
 }
 
+// Opt the track kernel into the device's full dynamic shared memory, once
+// per instantiation and device (never inside a stream capture's hot path).
+template <typename T, int VEC>
+static void prepare_track_kernel() {
+    static int done_for[64] = {0};
+    const DeviceInfo& d = device_info();
+    const int dev = d.device < 64 ? d.device : 63;
+    if (done_for[dev]) return;
+    cudaFuncSetAttribute(track_kernel<T, VEC>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         d.max_smem_optin);
+    done_for[dev] = 1;
+}
+
 template <typename T, int VEC>
 static int occupancy_blocks(size_t smem) {
     int b = 0;
-    cudaFuncSetAttribute(track_kernel<T, VEC>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         device_info().max_smem_optin);
+    prepare_track_kernel<T, VEC>();
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &b, track_kernel<T, VEC>, kTrackThreads, smem) != cudaSuccess)
         b = 1;
@@ -546,14 +558,13 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
         if (a.n_tiles < g) g = a.n_tiles;
         grid = (int)(g < 1 ? 1 : g);
     }
-    cudaFuncSetAttribute(track_kernel<T, VEC>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         device_info().max_smem_optin);
+    prepare_track_kernel<T, VEC>();
     track_kernel<T, VEC><<<grid, kTrackThreads, smem, st>>>(
         *prog, pk ? *pk : zero_pk, acc ? *acc : zero_acc, a);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_track launch: %s", cudaGetErrorString(e));
+    count_launches(1);
     return PHK_OK;
 }
 
@@ -665,6 +676,7 @@ int launch_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_slice_finalize launch: %s",
                          cudaGetErrorString(e));
+    count_launches(1);
     return PHK_OK;
 }
 
@@ -752,6 +764,7 @@ int launch_wake(const phk_wake_set* w, cudaStream_t st) {
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_wake launch: %s", cudaGetErrorString(e));
+    count_launches((int)any_conv + (int)any_dense);
     return PHK_OK;
 }
 
@@ -824,6 +837,7 @@ int launch_moments(const phk_slicer* sl, const void* z, int64_t n,
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_slice_moments launch: %s",
                          cudaGetErrorString(e));
+    count_launches(1);
     return PHK_OK;
 }
 

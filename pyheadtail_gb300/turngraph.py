@@ -1,0 +1,104 @@
+"""Whole-turn CUDA graphs.
+
+A PyHEADTAIL turn is a Python loop over elements; on the GPU each turn is
+only a handful of kernels (fused track, slice merge, wake), so for small
+bunches the host-side element code would dominate.  ``TurnGraph`` runs a
+few turns eagerly through the normal ``track(beam)`` API, checks that the
+turn's launch parameters have become stationary, captures one turn into a
+CUDA graph and then replays it: one graph launch per turn, no host work.
+
+Stationary means: constant energy (``p_increment == 0``; the reference's
+p0 setter round trip settles after two turns), fixed or bunch-independent
+cuts, and a wake history that no longer grows (single-turn wakes, or the
+multi-turn ring already full -- the ring position is then advanced on the
+device by capturing a full ring cycle).  While replaying, the host-side
+Python objects (slice-set deques, ages) are not updated; the device state
+(coordinates, moments ring, pending kicks) is.  After ``replay`` the beam
+and elements can be used eagerly again.
+"""
+import ctypes
+
+import torch
+
+from . import _native as N
+
+
+class _Recorder(object):
+    """Logs the pointer-free parameters of every native call of a turn."""
+
+    def __init__(self):
+        self.log = []
+
+    def __call__(self, name, args):
+        sig = [name]
+        for a in args:
+            obj = getattr(a, '_obj', None)
+            if isinstance(obj, N.Program):
+                sig.append(bytes(obj))
+            elif isinstance(obj, N.WakeSet):
+                sig.append((obj.n_kicks,) + tuple(
+                    (obj.kick[k].n_lags, obj.kick[k].factor)
+                    for k in range(obj.n_kicks)))
+            elif isinstance(obj, N.KickSet):
+                sig.append((obj.n_kicks, bytes(obj.slicer)))
+        self.log.append(tuple(sig))
+
+
+class TurnGraph(object):
+    """Capture / replay one turn of ``one_turn_map`` on ``beam``."""
+
+    def __init__(self, one_turn_map, beam, warmup_turns=3):
+        self.one_turn_map = list(one_turn_map)
+        self.beam = beam
+        self.warmup_turns = max(2, int(warmup_turns))
+        self.graph = None
+        self.turns_per_graph = 1
+
+    def _eager_turn(self):
+        for m in self.one_turn_map:
+            m.track(self.beam)
+
+    def _ring_cycle(self):
+        """Turns per graph: the longest moment-ring of a WakeField, so that
+        every replay leaves the ring position where it started."""
+        n = 1
+        for m in self.one_turn_map:
+            st = getattr(m, '_state', None)
+            if st is not None and st.n_ring > 1:
+                n = max(n, st.n_ring)
+        return n
+
+    def capture(self):
+        """Warm up eagerly, check stationarity, capture."""
+        logs = []
+        for t in range(self.warmup_turns):
+            rec = _Recorder()
+            N.RECORDERS.append(rec)
+            try:
+                self._eager_turn()
+            finally:
+                N.RECORDERS.remove(rec)
+            logs.append(rec.log)
+        if len(logs) >= 2 and logs[-1] != logs[-2]:
+            raise RuntimeError('turn parameters are not stationary (energy '
+                               'ramp, bunch-dependent cuts or a growing wake '
+                               'history); track eagerly instead')
+        self.turns_per_graph = self._ring_cycle()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(self.turns_per_graph):
+                    self._eager_turn()
+        torch.cuda.current_stream().wait_stream(s)
+        self.graph = g
+        return self
+
+    def replay(self, n_graphs=1):
+        """Run n_graphs * turns_per_graph turns."""
+        if self.graph is None:
+            self.capture()
+        for _ in range(n_graphs):
+            self.graph.replay()

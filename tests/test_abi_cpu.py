@@ -20,7 +20,7 @@ HEADER = os.path.join(ROOT, 'include', 'pyheadtail_gb300.h')
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
-    return sorted(set(re.findall(r'\bint\s+(phk_\w+)\s*\(', src)))
+    return sorted(set(re.findall(r'\bint(?:64_t)?\s+(phk_\w+)\s*\(', src)))
 
 
 @pytest.fixture(scope='module')

@@ -37,13 +37,30 @@ def rms_err(got, ref):
     return float(np.max(np.abs(got - ref)) / scale) if ref.size else 0.
 
 
-def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9):
+def dynamic_cuts(spec):
+    """True if a slicer of the case derives its cuts from the bunch
+    (n_sigma_z: mean and sigma of z; the reference sums them sequentially,
+    the GPU in a tree, so the cuts agree to ~1e-15 only)."""
+    sls = [el['slicer'] for el in spec['elements'] if 'slicer' in el]
+    return any(s['z_cuts'] is None and s['n_sigma_z'] for s in sls)
+
+
+def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9, emit_rtol=1e-7,
+            bins_rtol=0.0):
+    """Emittances per slice are sqrt(s11 s22 - s12^2) of covariances summed
+    in a different order than the reference's sequential loop; for slices
+    with few particles the determinant cancels by several orders, so they
+    get emit_rtol (the sums themselves agree to ~1e-15).  Bin edges are
+    bit-exact unless bins_rtol > 0 (dynamic cuts)."""
     for k, v in ref.items():
         if not k.startswith('t'):
             continue
         assert k in rec, '%s: missing %s' % (label, k)
         g = rec[k]
-        if k.endswith(('_idx', '_counts', '_gamma', '_p0', '_z_bins')):
+        if k.endswith('_z_bins') and bins_rtol > 0:
+            np.testing.assert_allclose(g, v, rtol=0, atol=bins_rtol *
+                                       np.max(np.abs(v)), err_msg=k)
+        elif k.endswith(('_idx', '_counts', '_gamma', '_p0', '_z_bins')):
             np.testing.assert_array_equal(np.asarray(g), v,
                                           err_msg='%s %s' % (label, k))
         elif k.endswith(('_mean_x', '_mean_y')) and np.ndim(v) == 0:
@@ -58,7 +75,8 @@ def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9):
             v = np.asarray(v, dtype=np.float64)
             g = np.asarray(g, dtype=np.float64)
             ok = np.isfinite(v)
-            tol = rtol if 'mean' in k else stat_rtol
+            tol = (rtol if 'mean' in k else
+                   emit_rtol if 'epsn' in k else stat_rtol)
             e = rms_err(g[ok], v[ok])
             assert e <= tol, '%s %s: rel err %.3g' % (label, k, e)
 
@@ -83,7 +101,8 @@ def test_golden_fixture_fp64(lib, path):
     coords = {k: ref['init_' + k] for k in COORDS}
     beam = G.make_beam(spec['beam'], coords)
     rec = G.run(spec, beam)
-    compare(rec, ref, os.path.basename(path))
+    compare(rec, ref, os.path.basename(path),
+            bins_rtol=1e-13 if dynamic_cuts(spec) else 0.0)
 
 
 def _oracle_vs_gpu(spec, n_turns, record_turns=None):
@@ -143,7 +162,6 @@ def test_edges_outside_nan_and_misaligned(lib):
     NaN z, and coordinate tensors that are views at an odd offset (not
     16-byte aligned: scalar path)."""
     import gpu_cases as G
-    from oracle import turn_loop as T
     from pyheadtail_gb300 import _engine as E
     import cases as C
     bp = C.beam_params(4000, 7)
@@ -173,11 +191,16 @@ def test_edges_outside_nan_and_misaligned(lib):
     want_i = np.where(np.isfinite(want) & (np.abs(want) < 2**31), want,
                       -2**31).astype(np.int64)
     np.testing.assert_array_equal(idx.astype(np.int64), want_i)
-    ob = T.Beam(coords, 1., 1., 1., 1., 27.7)
-    oss = T.UniformBinSlicer(S, z_cuts=cuts).slice(ob, ['mean_x', 'mean_y'])
+    # expected sums from the x86 conversion convention (NumPy on Arm maps
+    # NaN to 0 instead, which would put it into slice 0)
+    inside = (want_i >= 0) & (want_i < S)
+    counts = np.bincount(want_i[inside], minlength=S)
     np.testing.assert_array_equal(ss.n_macroparticles_per_slice.cpu().numpy(),
-                                  oss.n_macroparticles_per_slice)
-    assert rms_err(ss.mean_x.cpu().numpy(), oss.mean_x) <= RTOL
+                                  counts)
+    sums = np.bincount(want_i[inside], weights=coords['x'][inside],
+                       minlength=S)
+    mean = np.where(counts > 0, sums / np.maximum(counts, 1), 0.)
+    assert rms_err(ss.mean_x.cpu().numpy(), mean) <= RTOL
 
 
 def test_all_outside_and_empty_slices(lib):
