@@ -131,63 +131,94 @@ def build_oracle(w, coords):
 # ------------------------------------------------------------------ clocks
 
 class ClockSampler(object):
-    """nvidia-smi sampling during the timed region (clocks and throttle
-    reasons); never changes any GPU setting."""
+    """SM clock and clock-event reasons sampled every 10 ms during the timed
+    region through NVML (read-only queries; no setting is changed), with
+    nvidia-smi -lms 200 as the fallback when NVML cannot be loaded."""
 
-    Q = ('index,clocks.sm,clocks.max.sm,power.draw,'
-         'clocks_event_reasons.hw_slowdown,'
-         'clocks_event_reasons.hw_thermal_slowdown,'
-         'clocks_event_reasons.sw_thermal_slowdown,'
-         'clocks_event_reasons.sw_power_cap')
+    REASONS = {0x4: 'sw_power_cap', 0x8: 'hw_slowdown',
+               0x20: 'sw_thermal_slowdown', 0x40: 'hw_thermal_slowdown',
+               0x80: 'hw_power_brake_slowdown'}
 
     def __init__(self, device_index):
         self.dev = device_index
+        self.samples = []
+        self.max_mhz = None
+        self._stop = threading.Event()
+        self.t = None
         self.proc = None
-        self.lines = []
+
+    def _nvml(self):
+        import ctypes
+        lib = ctypes.CDLL('libnvidia-ml.so.1')
+        if lib.nvmlInit_v2() != 0:
+            raise OSError('nvmlInit failed')
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(self.dev, ctypes.byref(h)) != 0:
+            raise OSError('no NVML handle')
+        mx = ctypes.c_uint()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        self.max_mhz = float(mx.value)
+        reasons_fn = getattr(lib, 'nvmlDeviceGetCurrentClocksEventReasons',
+                             None) or lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        return lib, h, reasons_fn
+
+    def _loop_nvml(self, lib, h, reasons_fn):
+        import ctypes
+        clk = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        while not self._stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and \
+                    reasons_fn(h, ctypes.byref(rs)) == 0:
+                self.samples.append((float(clk.value), int(rs.value)))
+            self._stop.wait(0.01)
 
     def start(self):
         try:
+            lib, h, fn = self._nvml()
+            self.t = threading.Thread(target=self._loop_nvml,
+                                      args=(lib, h, fn), daemon=True)
+            self.t.start()
+            return
+        except (OSError, AttributeError):
+            pass
+        try:
             self.proc = subprocess.Popen(
-                ['nvidia-smi', '-i', str(self.dev), '--query-gpu=' + self.Q,
-                 '--format=csv,noheader,nounits', '-lms', '200'],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
+                ['nvidia-smi', '-i', str(self.dev),
+                 '--query-gpu=clocks.sm,clocks.max.sm,'
+                 'clocks_event_reasons.active', '--format=csv,noheader,nounits',
+                 '-lms', '200'], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._loop_smi, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
 
-    def _read(self):
+    def _loop_smi(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            f = [x.strip() for x in line.split(',')]
+            try:
+                self.max_mhz = float(f[1])
+                self.samples.append((float(f[0]), int(f[2], 16)))
+            except (ValueError, IndexError):
+                continue
 
     def stop(self):
-        if self.proc is None:
+        self._stop.set()
+        if self.proc is not None:
+            self.proc.terminate()
+        if self.t is not None:
+            self.t.join(timeout=5)
+        if not self.samples:
             return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        self.t.join(timeout=2)
-        sm, mx, reasons = [], [], set()
-        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
-                 'sw_power_cap']
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(',')]
-            if len(f) < 8:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, f[4:8]):
-                if v.lower().startswith('active'):
-                    reasons.add(nm)
-        if not sm:
-            return None
-        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': max(mx),
-                'reasons': sorted(reasons), 'samples': len(sm)}
+        sm = [s[0] for s in self.samples]
+        reasons = set()
+        for _, r in self.samples:
+            for bit, name in self.REASONS.items():
+                if r & bit:
+                    reasons.add(name)
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': self.max_mhz,
+                'reasons': sorted(reasons), 'samples': len(sm),
+                'source': 'nvml' if self.proc is None else 'nvidia-smi'}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -236,10 +267,11 @@ def time_form(w, coords, precision, steps, warmup, flush):
     graph_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     # the graph replays kernels captured through libphk: count them from
     # one eager turn (same sequence)
+    for m in elements:                  # settle the pending-kick pipeline
+        m.track(beam)
     n_eager0 = N.launch_count()
     for m in elements:
         m.track(beam)
-    beam._engine.flush()
     torch.cuda.synchronize()
     kernels_per_turn = N.launch_count() - n_eager0
     del n0
@@ -423,7 +455,7 @@ def run_reference(a, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=50)
+    ap.add_argument('--steps', type=int, default=400)
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', choices=['ours', 'reference'], default='ours')
     ap.add_argument('--workload', choices=sorted(WORKLOADS), default='c2')

@@ -68,18 +68,25 @@ class TurnGraph(object):
                 n = max(n, st.n_ring)
         return n
 
-    def capture(self):
-        """Warm up eagerly, check stationarity, capture."""
-        logs = []
-        for t in range(self.warmup_turns):
-            rec = _Recorder()
-            N.RECORDERS.append(rec)
-            try:
-                self._eager_turn()
-            finally:
-                N.RECORDERS.remove(rec)
-            logs.append(rec.log)
-        if len(logs) >= 2 and logs[-1] != logs[-2]:
+    def _logged_turn(self):
+        rec = _Recorder()
+        N.RECORDERS.append(rec)
+        try:
+            self._eager_turn()
+        finally:
+            N.RECORDERS.remove(rec)
+        return rec.log
+
+    def capture(self, max_extra_turns=20):
+        """Warm up eagerly (at least warmup_turns, then until two
+        consecutive turns launch identical parameters), then capture."""
+        prev = None
+        for t in range(self.warmup_turns + max_extra_turns):
+            log = self._logged_turn()
+            if t + 1 >= self.warmup_turns and log == prev:
+                break
+            prev = log
+        else:
             raise RuntimeError('turn parameters are not stationary (energy '
                                'ramp, bunch-dependent cuts or a growing wake '
                                'history); track eagerly instead')
