@@ -14,6 +14,17 @@
 namespace phk {
 
 // ===================================================================
+// particle tiles: VEC particles per thread, one register array per
+// coordinate; every op below works op-major / particle-minor, reading its
+// parameters once per tile
+// ===================================================================
+
+template <typename T, int VEC>
+struct Tile {
+    T c[6][VEC];
+};
+
+// ===================================================================
 // element arithmetic, plain FP64 form (reference evaluation order)
 // ===================================================================
 
@@ -37,130 +48,184 @@ __device__ __forceinline__ double amp_action(double c1, double twoa, double b,
     return mul(0.5, s);
 }
 
-__device__ __forceinline__ double ij_term(const double* p, int mask, int bi,
-                                          int bj, double cc, double ss) {
-    const bool hi = (mask >> bi) & 1, hj = (mask >> bj) & 1;
-    if (hi && hj) return add(mul(p[bi], cc), mul(p[bj], ss));
-    if (hi) return mul(p[bi], cc);
-    if (hj) return mul(p[bj], ss);
+__device__ __forceinline__ double ij_term(double I, double J, bool hi,
+                                          bool hj, double cc, double ss) {
+    if (hi && hj) return add(mul(I, cc), mul(J, ss));
+    if (hi) return mul(I, cc);
+    if (hj) return mul(J, ss);
     return 0.0;
 }
 
-__device__ __forceinline__ void op_transverse_f64(const phk_op& op,
-                                                  const phk_program& prog,
-                                                  double& x, double& xp,
-                                                  double& y, double& yp,
-                                                  double dp) {
+template <int VEC>
+__device__ __forceinline__ void op_transverse(const phk_op& op,
+                                              const phk_program& prog,
+                                              Tile<double, VEC>& t) {
     const double* p = op.p;
-    double M00, M01, M10, M11, M22, M23, M32, M33;
-    if (op.flags & PHK_FLAG_DETUNED) {
-        double phx = p[20], phy = p[21];
-        for (int d = 0; d < op.det_count; ++d) {
-            const phk_detuner& dt = prog.det[op.det_begin + d];
-            if (dt.kind == PHK_DET_CHROMA) {
-                phx = add(phx, chroma_poly(dt.c, dt.nx, dt.zx, dp));
-                phy = add(phy, chroma_poly(dt.c + 8, dt.ny, dt.zy, dp));
-            } else {
-                const double* c = dt.c;
-                const double Jx = amp_action(c[4], c[5], c[6], x, xp);
-                const double Jy = amp_action(c[7], c[8], c[9], y, yp);
-                phx = add(phx, dvd(add(mul(c[0], Jx), mul(c[2], Jy)), c[10]));
-                phy = add(phy, dvd(add(mul(c[1], Jy), mul(c[3], Jx)), c[10]));
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+    const double Dx0 = p[16], Dx1 = p[17], Dy0 = p[18], Dy1 = p[19];
+    double (&x)[VEC] = t.c[PHK_X];
+    double (&xp)[VEC] = t.c[PHK_XP];
+    double (&y)[VEC] = t.c[PHK_Y];
+    double (&yp)[VEC] = t.c[PHK_YP];
+    const double (&dp)[VEC] = t.c[PHK_DP];
+    if (!(op.flags & PHK_FLAG_DETUNED)) {
+        const double M00 = p[0], M01 = p[1], M10 = p[2], M11 = p[3];
+        const double M22 = p[4], M23 = p[5], M32 = p[6], M33 = p[7];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            if (disp) {
+                x[j] = sub(x[j], mul(Dx0, dp[j]));
+                y[j] = sub(y[j], mul(Dy0, dp[j]));
+            }
+            const double nx = add(mul(M00, x[j]), mul(M01, xp[j]));
+            const double nxp = add(mul(M10, x[j]), mul(M11, xp[j]));
+            const double ny = add(mul(M22, y[j]), mul(M23, yp[j]));
+            const double nyp = add(mul(M32, y[j]), mul(M33, yp[j]));
+            x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
+            if (disp) {
+                x[j] = add(x[j], mul(Dx1, dp[j]));
+                y[j] = add(y[j], mul(Dy1, dp[j]));
             }
         }
-        phx = mul(phx, p[22]);
-        phy = mul(phy, p[22]);
-        double sx, cx, sy, cy;
-        sincos(phx, &sx, &cx);
-        sincos(phy, &sy, &cy);
-        const int m = op.ij_mask;
-        M00 = ij_term(p, m, 0, 8, cx, sx);
-        M01 = ij_term(p, m, 1, 9, cx, sx);
-        M10 = ij_term(p, m, 2, 10, cx, sx);
-        M11 = ij_term(p, m, 3, 11, cx, sx);
-        M22 = ij_term(p, m, 4, 12, cy, sy);
-        M23 = ij_term(p, m, 5, 13, cy, sy);
-        M32 = ij_term(p, m, 6, 14, cy, sy);
-        M33 = ij_term(p, m, 7, 15, cy, sy);
-    } else {
-        M00 = p[0]; M01 = p[1]; M10 = p[2]; M11 = p[3];
-        M22 = p[4]; M23 = p[5]; M32 = p[6]; M33 = p[7];
+        return;
     }
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = sub(x, mul(p[16], dp));
-        y = sub(y, mul(p[18], dp));
-    }
-    const double nx = add(mul(M00, x), mul(M01, xp));
-    const double nxp = add(mul(M10, x), mul(M11, xp));
-    const double ny = add(mul(M22, y), mul(M23, yp));
-    const double nyp = add(mul(M32, y), mul(M33, yp));
-    x = nx; xp = nxp; y = ny; yp = nyp;
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = add(x, mul(p[17], dp));
-        y = add(y, mul(p[19], dp));
-    }
-}
-
-__device__ __forceinline__ void op_drift_f64(const phk_op& op, double& z,
-                                             double dp) {
-    const double* p = op.p;
-    const double zz = (op.flags & PHK_FLAG_SHRINK) ? mul(p[0], z) : z;
-    z = sub(zz, mul(mul(p[1], dp), p[2]));
-}
-
-__device__ __forceinline__ void op_rfkick_f64(const phk_op& op, double& x,
-                                              double& y, double z,
-                                              double& dp) {
-    const double* p = op.p;
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = sub(x, mul(p[9], dp));
-        y = sub(y, mul(p[10], dp));
-    }
-    double phi = mul(p[0], dvd(mul(p[1], z), p[2]));
-    if (op.flags & PHK_FLAG_PHI_OFFSET) phi = add(phi, p[3]);
-    if (op.flags & PHK_FLAG_PHI_LOCK) phi = add(phi, p[4]);
-    double t = mul(p[5], sin(phi));
-    if (op.flags & PHK_FLAG_P_INC) t = sub(t, p[7]);
-    dp = dvd(add(mul(dp, p[6]), t), p[8]);
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = add(x, mul(p[9], dp));
-        y = add(y, mul(p[10], dp));
-    }
-}
-
-__device__ __forceinline__ void op_linear_long_f64(const phk_op& op,
-                                                   double& x, double& y,
-                                                   double& z, double& dp) {
-    const double* p = op.p;
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = sub(x, mul(p[3], dp));
-        y = sub(y, mul(p[4], dp));
-    }
-    const double z0 = z, dp0 = dp;
-    z = sub(mul(z0, p[0]), mul(mul(p[2], dp0), p[1]));
-    dp = add(mul(dp0, p[0]), mul(dvd(z0, p[2]), p[1]));
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = add(x, mul(p[3], dp));
-        y = add(y, mul(p[4], dp));
-    }
-}
-
-__device__ __forceinline__ void apply_op(const phk_op& op,
-                                         const phk_program& prog, double& x,
-                                         double& xp, double& y, double& yp,
-                                         double& z, double& dp) {
-    switch (op.kind) {
-        case PHK_OP_TRANSVERSE: op_transverse_f64(op, prog, x, xp, y, yp, dp); break;
-        case PHK_OP_DRIFT: op_drift_f64(op, z, dp); break;
-        case PHK_OP_RF_KICK: op_rfkick_f64(op, x, y, z, dp); break;
-        case PHK_OP_LINEAR_LONG: op_linear_long_f64(op, x, y, z, dp); break;
-        case PHK_OP_SCALE_TRANS: {
-            const double f = op.p[0];
-            x = mul(x, f); xp = mul(xp, f); y = mul(y, f); yp = mul(yp, f);
-            break;
+    double phx[VEC], phy[VEC];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) { phx[j] = p[20]; phy[j] = p[21]; }
+    for (int d = 0; d < op.det_count; ++d) {
+        const phk_detuner& dt = prog.det[op.det_begin + d];
+        if (dt.kind == PHK_DET_CHROMA) {
+            const int nx = dt.nx, ny = dt.ny, zx = dt.zx, zy = dt.zy;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                phx[j] = add(phx[j], chroma_poly(dt.c, nx, zx, dp[j]));
+                phy[j] = add(phy[j], chroma_poly(dt.c + 8, ny, zy, dp[j]));
+            }
+        } else {
+            const double ax = dt.c[0], ay = dt.c[1], axy = dt.c[2], ayx = dt.c[3];
+            const double c1x = dt.c[4], tax = dt.c[5], bx = dt.c[6];
+            const double c1y = dt.c[7], tay = dt.c[8], by = dt.c[9];
+            const double p0 = dt.c[10];
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                const double Jx = amp_action(c1x, tax, bx, x[j], xp[j]);
+                const double Jy = amp_action(c1y, tay, by, y[j], yp[j]);
+                phx[j] = add(phx[j], dvd(add(mul(ax, Jx), mul(axy, Jy)), p0));
+                phy[j] = add(phy[j], dvd(add(mul(ay, Jy), mul(ayx, Jx)), p0));
+            }
         }
-        default: break;
     }
+    const double twopi = p[22];
+    const int m = op.ij_mask;
+    double I[8], J[8];
+    bool hI[8], hJ[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        I[e] = p[e]; J[e] = p[8 + e];
+        hI[e] = (m >> e) & 1; hJ[e] = (m >> (8 + e)) & 1;
+    }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        double sx, cx, sy, cy;
+        sincos(mul(phx[j], twopi), &sx, &cx);
+        sincos(mul(phy[j], twopi), &sy, &cy);
+        const double M00 = ij_term(I[0], J[0], hI[0], hJ[0], cx, sx);
+        const double M01 = ij_term(I[1], J[1], hI[1], hJ[1], cx, sx);
+        const double M10 = ij_term(I[2], J[2], hI[2], hJ[2], cx, sx);
+        const double M11 = ij_term(I[3], J[3], hI[3], hJ[3], cx, sx);
+        const double M22 = ij_term(I[4], J[4], hI[4], hJ[4], cy, sy);
+        const double M23 = ij_term(I[5], J[5], hI[5], hJ[5], cy, sy);
+        const double M32 = ij_term(I[6], J[6], hI[6], hJ[6], cy, sy);
+        const double M33 = ij_term(I[7], J[7], hI[7], hJ[7], cy, sy);
+        if (disp) {
+            x[j] = sub(x[j], mul(Dx0, dp[j]));
+            y[j] = sub(y[j], mul(Dy0, dp[j]));
+        }
+        const double nx = add(mul(M00, x[j]), mul(M01, xp[j]));
+        const double nxp = add(mul(M10, x[j]), mul(M11, xp[j]));
+        const double ny = add(mul(M22, y[j]), mul(M23, yp[j]));
+        const double nyp = add(mul(M32, y[j]), mul(M33, yp[j]));
+        x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
+        if (disp) {
+            x[j] = add(x[j], mul(Dx1, dp[j]));
+            y[j] = add(y[j], mul(Dy1, dp[j]));
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_drift(const phk_op& op,
+                                         Tile<double, VEC>& t) {
+    const double br = op.p[0], eta0 = op.p[1], L = op.p[2];
+    const bool shrink = op.flags & PHK_FLAG_SHRINK;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        const double z = t.c[PHK_Z][j];
+        const double zz = shrink ? mul(br, z) : z;
+        t.c[PHK_Z][j] = sub(zz, mul(mul(eta0, t.c[PHK_DP][j]), L));
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_rfkick(const phk_op& op,
+                                          Tile<double, VEC>& t) {
+    const double* p = op.p;
+    const int f = op.flags;
+    const double h = p[0], twopi = p[1], C = p[2], off = p[3], lock = p[4];
+    const double A = p[5], p0o = p[6], pinc = p[7], p0n = p[8];
+    const double Dx = p[9], Dy = p[10];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        double& dp = t.c[PHK_DP][j];
+        if (f & PHK_FLAG_DISPERSION) {
+            t.c[PHK_X][j] = sub(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = sub(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+        double phi = mul(h, dvd(mul(twopi, t.c[PHK_Z][j]), C));
+        if (f & PHK_FLAG_PHI_OFFSET) phi = add(phi, off);
+        if (f & PHK_FLAG_PHI_LOCK) phi = add(phi, lock);
+        double s = mul(A, sin(phi));
+        if (f & PHK_FLAG_P_INC) s = sub(s, pinc);
+        dp = dvd(add(mul(dp, p0o), s), p0n);
+        if (f & PHK_FLAG_DISPERSION) {
+            t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_linear_long(const phk_op& op,
+                                               Tile<double, VEC>& t) {
+    const double* p = op.p;
+    const double cs = p[0], sn = p[1], lf = p[2], Dx = p[3], Dy = p[4];
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        double& z = t.c[PHK_Z][j];
+        double& dp = t.c[PHK_DP][j];
+        if (disp) {
+            t.c[PHK_X][j] = sub(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = sub(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+        const double z0 = z, dp0 = dp;
+        z = sub(mul(z0, cs), mul(mul(lf, dp0), sn));
+        dp = add(mul(dp0, cs), mul(dvd(z0, lf), sn));
+        if (disp) {
+            t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_scale(const phk_op& op,
+                                         Tile<double, VEC>& t) {
+    const double f = op.p[0];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) t.c[q][j] = mul(t.c[q][j], f);
 }
 
 // ===================================================================
@@ -176,118 +241,230 @@ __device__ __forceinline__ float chroma_poly_f32(const float* c, int n, int z,
     return r;
 }
 
-__device__ __forceinline__ void op_transverse_f32(const phk_op& op,
-                                                  const phk_program& prog,
-                                                  float& x, float& xp,
-                                                  float& y, float& yp,
-                                                  float dp) {
+template <int VEC>
+__device__ __forceinline__ void op_transverse(const phk_op& op,
+                                              const phk_program& prog,
+                                              Tile<float, VEC>& t) {
     const float* p = reinterpret_cast<const float*>(op.p);
-    float M00, M01, M10, M11, M22, M23, M32, M33;
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+    const float Dx0 = p[32], Dx1 = p[33], Dy0 = p[34], Dy1 = p[35];
+    float (&x)[VEC] = t.c[PHK_X];
+    float (&xp)[VEC] = t.c[PHK_XP];
+    float (&y)[VEC] = t.c[PHK_Y];
+    float (&yp)[VEC] = t.c[PHK_YP];
+    const float (&dp)[VEC] = t.c[PHK_DP];
+    float M[8][VEC];
     if (op.flags & PHK_FLAG_DETUNED) {
-        float dqx = 0.f, dqy = 0.f;
+        float dqx[VEC], dqy[VEC];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) { dqx[j] = 0.f; dqy[j] = 0.f; }
         for (int d = 0; d < op.det_count; ++d) {
             const phk_detuner& dt = prog.det[op.det_begin + d];
             const float* c = reinterpret_cast<const float*>(dt.c);
             if (dt.kind == PHK_DET_CHROMA) {
-                dqx += chroma_poly_f32(c, dt.nx, dt.zx, dp);
-                dqy += chroma_poly_f32(c + 8, dt.ny, dt.zy, dp);
+                const int nx = dt.nx, ny = dt.ny, zx = dt.zx, zy = dt.zy;
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) {
+                    dqx[j] += chroma_poly_f32(c, nx, zx, dp[j]);
+                    dqy[j] += chroma_poly_f32(c + 8, ny, zy, dp[j]);
+                }
             } else {
                 // c = dapp_x/p0, dapp_y/p0, dapp_xy/p0, dapp_yx/p0,
                 //     (1+ax^2)/bx, 2ax, bx, (1+ay^2)/by, 2ay, by
-                const float Jx = 0.5f * fmaf(c[6] * xp, xp, fmaf(c[5] * x, xp, c[4] * x * x));
-                const float Jy = 0.5f * fmaf(c[9] * yp, yp, fmaf(c[8] * y, yp, c[7] * y * y));
-                dqx += fmaf(c[0], Jx, c[2] * Jy);
-                dqy += fmaf(c[1], Jy, c[3] * Jx);
+                const float ax = c[0], ay = c[1], axy = c[2], ayx = c[3];
+                const float c1x = c[4], tax = c[5], bx = c[6];
+                const float c1y = c[7], tay = c[8], by = c[9];
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) {
+                    const float Jx = 0.5f * fmaf(bx * xp[j], xp[j],
+                                                 fmaf(tax * x[j], xp[j], c1x * x[j] * x[j]));
+                    const float Jy = 0.5f * fmaf(by * yp[j], yp[j],
+                                                 fmaf(tay * y[j], yp[j], c1y * y[j] * y[j]));
+                    dqx[j] += fmaf(ax, Jx, axy * Jy);
+                    dqy[j] += fmaf(ay, Jy, ayx * Jx);
+                }
             }
         }
-        float sx, cx, sy, cy;
-        sincos_turns(p[16], p[17], dqx, &sx, &cx);
-        sincos_turns(p[18], p[19], dqy, &sy, &cy);
-        M00 = fmaf(p[0], cx, p[8] * sx);
-        M01 = fmaf(p[1], cx, p[9] * sx);
-        M10 = fmaf(p[2], cx, p[10] * sx);
-        M11 = fmaf(p[3], cx, p[11] * sx);
-        M22 = fmaf(p[4], cy, p[12] * sy);
-        M23 = fmaf(p[5], cy, p[13] * sy);
-        M32 = fmaf(p[6], cy, p[14] * sy);
-        M33 = fmaf(p[7], cy, p[15] * sy);
+        const float qxh = p[16], qxl = p[17], qyh = p[18], qyl = p[19];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            float sx, cx, sy, cy;
+            sincos_turns(qxh, qxl, dqx[j], &sx, &cx);
+            sincos_turns(qyh, qyl, dqy[j], &sy, &cy);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                M[e][j] = fmaf(p[e], cx, p[8 + e] * sx);
+                M[4 + e][j] = fmaf(p[4 + e], cy, p[12 + e] * sy);
+            }
+        }
     } else {
-        M00 = p[0]; M01 = p[1]; M10 = p[2]; M11 = p[3];
-        M22 = p[4]; M23 = p[5]; M32 = p[6]; M33 = p[7];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) M[e][j] = p[e];
     }
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = fmaf(-p[32], dp, x);
-        y = fmaf(-p[34], dp, y);
-    }
-    const float nx = fmaf(M00, x, M01 * xp);
-    const float nxp = fmaf(M10, x, M11 * xp);
-    const float ny = fmaf(M22, y, M23 * yp);
-    const float nyp = fmaf(M32, y, M33 * yp);
-    x = nx; xp = nxp; y = ny; yp = nyp;
-    if (op.flags & PHK_FLAG_DISPERSION) {
-        x = fmaf(p[33], dp, x);
-        y = fmaf(p[35], dp, y);
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        if (disp) {
+            x[j] = fmaf(-Dx0, dp[j], x[j]);
+            y[j] = fmaf(-Dy0, dp[j], y[j]);
+        }
+        const float nx = fmaf(M[0][j], x[j], M[1][j] * xp[j]);
+        const float nxp = fmaf(M[2][j], x[j], M[3][j] * xp[j]);
+        const float ny = fmaf(M[4][j], y[j], M[5][j] * yp[j]);
+        const float nyp = fmaf(M[6][j], y[j], M[7][j] * yp[j]);
+        x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
+        if (disp) {
+            x[j] = fmaf(Dx1, dp[j], x[j]);
+            y[j] = fmaf(Dy1, dp[j], y[j]);
+        }
     }
 }
 
-__device__ __forceinline__ void apply_op(const phk_op& op,
-                                         const phk_program& prog, float& x,
-                                         float& xp, float& y, float& yp,
-                                         float& z, float& dp) {
+template <int VEC>
+__device__ __forceinline__ void op_drift(const phk_op& op,
+                                         Tile<float, VEC>& t) {
     const float* p = reinterpret_cast<const float*>(op.p);
-    switch (op.kind) {
-        case PHK_OP_TRANSVERSE: op_transverse_f32(op, prog, x, xp, y, yp, dp); break;
-        case PHK_OP_DRIFT:
-            // z = beta_ratio * z - (eta0 * L) * dp
-            z = fmaf(-p[1], dp, (op.flags & PHK_FLAG_SHRINK) ? p[0] * z : z);
-            break;
-        case PHK_OP_RF_KICK: {
-            // p: h/C (hi, lo) turns per metre, (phi_offset+phi_lock)/2pi
-            // (hi, lo), A/p0_new, p0_old/p0_new, p_inc/p0_new, D_x, D_y
-            if (op.flags & PHK_FLAG_DISPERSION) {
-                x = fmaf(-p[8], dp, x);
-                y = fmaf(-p[9], dp, y);
-            }
-            const float s = sin_turns_of_product(z, p[0], p[1], p[2], p[3]);
-            dp = fmaf(p[4], s, fmaf(dp, p[5], -p[6]));
-            if (op.flags & PHK_FLAG_DISPERSION) {
-                x = fmaf(p[8], dp, x);
-                y = fmaf(p[9], dp, y);
-            }
-            break;
-        }
-        case PHK_OP_LINEAR_LONG: {
-            // p: cos, sin, longfac, 1/longfac, D_x, D_y
-            if (op.flags & PHK_FLAG_DISPERSION) {
-                x = fmaf(-p[4], dp, x);
-                y = fmaf(-p[5], dp, y);
-            }
-            const float z0 = z, dp0 = dp;
-            z = fmaf(z0, p[0], -(p[2] * dp0) * p[1]);
-            dp = fmaf(dp0, p[0], (z0 * p[3]) * p[1]);
-            if (op.flags & PHK_FLAG_DISPERSION) {
-                x = fmaf(p[4], dp, x);
-                y = fmaf(p[5], dp, y);
-            }
-            break;
-        }
-        case PHK_OP_SCALE_TRANS: {
-            const float f = p[0];
-            x *= f; xp *= f; y *= f; yp *= f;
-            break;
-        }
-        default: break;
+    const float br = p[0], etaL = p[1];
+    const bool shrink = op.flags & PHK_FLAG_SHRINK;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        // z = beta_ratio * z - (eta0 * L) * dp
+        const float z = t.c[PHK_Z][j];
+        t.c[PHK_Z][j] = fmaf(-etaL, t.c[PHK_DP][j], shrink ? br * z : z);
     }
 }
+
+template <int VEC>
+__device__ __forceinline__ void op_rfkick(const phk_op& op,
+                                          Tile<float, VEC>& t) {
+    // p: h/C (hi, lo) turns per metre, (phi_offset+phi_lock)/2pi (hi, lo),
+    //    A/p0_new, p0_old/p0_new, p_inc/p0_new, -, D_x, D_y
+    const float* p = reinterpret_cast<const float*>(op.p);
+    const float mh = p[0], ml = p[1], oh = p[2], ol = p[3];
+    const float A = p[4], ratio = p[5], pinc = p[6], Dx = p[8], Dy = p[9];
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        float& dp = t.c[PHK_DP][j];
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(-Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
+        }
+        const float s = sin_turns_of_product(t.c[PHK_Z][j], mh, ml, oh, ol);
+        dp = fmaf(A, s, fmaf(dp, ratio, -pinc));
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_linear_long(const phk_op& op,
+                                               Tile<float, VEC>& t) {
+    // p: cos, sin, longfac, 1/longfac, D_x, D_y
+    const float* p = reinterpret_cast<const float*>(op.p);
+    const float cs = p[0], sn = p[1], lf = p[2], ilf = p[3];
+    const float Dx = p[4], Dy = p[5];
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        float& z = t.c[PHK_Z][j];
+        float& dp = t.c[PHK_DP][j];
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(-Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
+        }
+        const float z0 = z, dp0 = dp;
+        z = fmaf(z0, cs, -(lf * dp0) * sn);
+        dp = fmaf(dp0, cs, (z0 * ilf) * sn);
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_scale(const phk_op& op,
+                                         Tile<float, VEC>& t) {
+    const float f = reinterpret_cast<const float*>(op.p)[0];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) t.c[q][j] *= f;
+}
+
+// one dispatch per op per tile (uniform across the CTA)
+template <typename T, int VEC>
+__device__ __forceinline__ void run_program(const phk_program& prog,
+                                            Tile<T, VEC>& t) {
+    for (int o = 0; o < prog.n_ops; ++o) {
+        const phk_op& op = prog.op[o];
+        switch (op.kind) {
+            case PHK_OP_TRANSVERSE: op_transverse<VEC>(op, prog, t); break;
+            case PHK_OP_DRIFT: op_drift<VEC>(op, t); break;
+            case PHK_OP_RF_KICK: op_rfkick<VEC>(op, t); break;
+            case PHK_OP_LINEAR_LONG: op_linear_long<VEC>(op, t); break;
+            case PHK_OP_SCALE_TRANS: op_scale<VEC>(op, t); break;
+            default: break;
+        }
+    }
+}
+
+// ===================================================================
+// per-slice accumulation in shared memory
+//   FP64 form: per-warp (or per-CTA) histograms of double sums
+//   FP32 form: per-warp histograms of Kahan-compensated float sums; the
+//              (sum, compensation) pair of a bin is one 64-bit word updated
+//              with a 64-bit compare-and-swap, so each update is atomic
+// ===================================================================
+
+template <typename T>
+struct Hist;
+
+template <>
+struct Hist<double> {
+    using Word = double;
+    static constexpr int kWordBytes = 8;
+    static __device__ __forceinline__ void zero(Word* w) { *w = 0.0; }
+    static __device__ __forceinline__ void add(Word* w, double v) {
+        atomicAdd(w, v);
+    }
+    static __device__ __forceinline__ double value(const Word* w) { return *w; }
+};
+
+template <>
+struct Hist<float> {
+    using Word = unsigned long long;  // low 32 bits: sum, high: compensation
+    static constexpr int kWordBytes = 8;
+    static __device__ __forceinline__ void zero(Word* w) { *w = 0ull; }
+    static __device__ __forceinline__ void add(Word* w, float v) {
+        Word old = *w, assumed;
+        do {
+            assumed = old;
+            const float s = __uint_as_float((unsigned)(assumed & 0xffffffffu));
+            const float c = __uint_as_float((unsigned)(assumed >> 32));
+            // Kahan (1965) compensated summation step
+            const float yk = v - c;
+            const float tk = s + yk;
+            const float cn = (tk - s) - yk;
+            const Word nw = (Word)__float_as_uint(tk) |
+                            ((Word)__float_as_uint(cn) << 32);
+            old = atomicCAS(w, assumed, nw);
+        } while (old != assumed);
+    }
+    static __device__ __forceinline__ double value(const Word* w) {
+        const float s = __uint_as_float((unsigned)(*w & 0xffffffffu));
+        const float c = __uint_as_float((unsigned)(*w >> 32));
+        return (double)s - (double)c;
+    }
+};
 
 // ===================================================================
 // the fused track kernel
 // ===================================================================
-
-template <typename T>
-struct AccumType { using type = double; };
-template <>
-struct AccumType<float> { using type = float; };
 
 template <typename T, int VEC>
 struct VecIO;
@@ -325,17 +502,42 @@ struct TrackArgs {
     int32_t has_acc;
     int32_t load_mask;
     int32_t store_mask;
+    int32_t n_hist;      // histogram copies per CTA (1 or warps per CTA)
+    int32_t kicks_smem;  // kick tables staged in shared memory
 };
 
-__device__ __forceinline__ double tmul(double a, double b) { return mul(a, b); }
-__device__ __forceinline__ double tadd(double a, double b) { return add(a, b); }
-__device__ __forceinline__ float tmul(float a, float b) { return a * b; }
-__device__ __forceinline__ float tadd(float a, float b) { return a + b; }
+template <typename T>
+__device__ __forceinline__ T tadd(T a, T b);
+template <>
+__device__ __forceinline__ double tadd<double>(double a, double b) { return add(a, b); }
+template <>
+__device__ __forceinline__ float tadd<float>(float a, float b) { return a + b; }
+template <typename T>
+__device__ __forceinline__ T tmul(T a, T b);
+template <>
+__device__ __forceinline__ double tmul<double>(double a, double b) { return mul(a, b); }
+template <>
+__device__ __forceinline__ float tmul<float>(float a, float b) { return a * b; }
+
+// shared memory layout, in this order (every region 16-byte aligned):
+//   histogram words  [3][n_hist][Sa]   (sum x, sum y as Hist<T>::Word; count
+//                                       as int in the third region)
+//   accumulation edges [Sa + 1] T, pending-kick edges [Sp + 1] T,
+//   kick tables [n_kicks][Sp] T (when staged)
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
 template <typename T>
-__device__ __forceinline__ T kick_value(const phk_kick_set& pk, int k,
-                                        int s) {
-    return __ldg(reinterpret_cast<const T*>(pk.kick[k]) + s);
+__host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
+                                                    int n_kicks, int kicks_smem,
+                                                    size_t* off) {
+    size_t b = 0;
+    off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x
+    off[1] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum y
+    off[2] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // count
+    off[3] = b; b = align16(b + sizeof(T) * (Sa > 0 ? Sa + 1 : 0));
+    off[4] = b; b = align16(b + sizeof(T) * (Sp > 0 ? Sp + 1 : 0));
+    off[5] = b; b = align16(b + (kicks_smem ? sizeof(T) * (size_t)n_kicks * Sp : 0));
+    return b;
 }
 
 template <typename T, int VEC>
@@ -343,104 +545,121 @@ __global__ void __launch_bounds__(kTrackThreads)
 track_kernel(const __grid_constant__ phk_program prog,
              const __grid_constant__ phk_kick_set pk,
              const __grid_constant__ phk_accum acc, const TrackArgs a) {
-    using AccT = typename AccumType<T>::type;
+    using W = typename Hist<T>::Word;
     extern __shared__ __align__(16) unsigned char smem[];
     const int Sa = a.has_acc ? acc.slicer.n_slices : 0;
     const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
-    AccT* hsx = reinterpret_cast<AccT*>(smem);
-    AccT* hsy = hsx + Sa;
-    T* eacc = reinterpret_cast<T*>(hsy + Sa);
-    T* epk = eacc + (a.has_acc ? Sa + 1 : 0);
-    int* hcnt = reinterpret_cast<int*>(epk + (a.has_pk ? Sp + 1 : 0));
+    const int nk = a.has_pk ? pk.n_kicks : 0;
+    size_t off[6];
+    track_smem_layout<T>(Sa, Sp, a.n_hist, nk, a.kicks_smem, off);
+    W* hsx = reinterpret_cast<W*>(smem + off[0]);
+    W* hsy = reinterpret_cast<W*>(smem + off[1]);
+    int* hcnt = reinterpret_cast<int*>(smem + off[2]);
+    T* eacc = reinterpret_cast<T*>(smem + off[3]);
+    T* epk = reinterpret_cast<T*>(smem + off[4]);
+    T* ktab = reinterpret_cast<T*>(smem + off[5]);
 
     const int tid = threadIdx.x;
     if (a.has_acc) {
         const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
         for (int i = tid; i <= Sa; i += blockDim.x) eacc[i] = e[i];
-        for (int i = tid; i < Sa; i += blockDim.x) {
-            hsx[i] = AccT(0); hsy[i] = AccT(0); hcnt[i] = 0;
+        for (int i = tid; i < a.n_hist * Sa; i += blockDim.x) {
+            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i); hcnt[i] = 0;
         }
     }
     if (a.has_pk) {
         const T* e = reinterpret_cast<const T*>(pk.slicer.edges);
         for (int i = tid; i <= Sp; i += blockDim.x) epk[i] = e[i];
+        if (a.kicks_smem)
+            for (int i = tid; i < nk * Sp; i += blockDim.x) {
+                const int k = i / Sp;
+                ktab[i] = reinterpret_cast<const T*>(pk.kick[k])[i - k * Sp];
+            }
     }
     __syncthreads();
+
+    // first-estimate parameters of the two bin searches, from the tables
+    T pk_tail = T(0), pk_iw = T(0), ac_tail = T(0), ac_iw = T(0);
+    if (a.has_pk) {
+        pk_tail = epk[0];
+        const T span = epk[Sp] - epk[0];
+        pk_iw = span > T(0) ? T(Sp) / span : T(0);
+    }
+    if (a.has_acc) {
+        ac_tail = eacc[0];
+        const T span = eacc[Sa] - eacc[0];
+        ac_iw = span > T(0) ? T(Sa) / span : T(0);
+    }
+    const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
+    W* my_sx = hsx + h * Sa;
+    W* my_sy = hsy + h * Sa;
+    int* my_cnt = hcnt + h * Sa;
 
     T* cp[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) cp[q] = reinterpret_cast<T*>(a.c[q]);
-    const T pk_tail = T(pk.slicer.est_tail), pk_iw = T(pk.slicer.est_inv_w);
-    const T ac_tail = T(acc.slicer.est_tail), ac_iw = T(acc.slicer.est_inv_w);
 
     for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
         const int64_t i0 = (tile * blockDim.x + tid) * VEC;
         if (i0 >= a.n) continue;
         const bool full = i0 + VEC <= a.n;
-        T v[6][VEC];
+        Tile<T, VEC> t;
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             if (!((a.load_mask >> q) & 1)) {
 #pragma unroll
-                for (int j = 0; j < VEC; ++j) v[q][j] = T(0);
+                for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
                 continue;
             }
             if (full) {
-                VecIO<T, VEC>::ld(cp[q] + i0, v[q]);
+                VecIO<T, VEC>::ld(cp[q] + i0, t.c[q]);
             } else {
 #pragma unroll
                 for (int j = 0; j < VEC; ++j)
-                    v[q][j] = (i0 + j < a.n) ? cp[q][i0 + j] : T(0);
+                    t.c[q][j] = (i0 + j < a.n) ? cp[q][i0 + j] : T(0);
             }
         }
         // 1. wake kicks of the previous WakeField.track, in kick order
         if (a.has_pk) {
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
-                const int s = slice_of<T>(v[PHK_Z][j], Sp, pk.slicer.negate,
+                const int s = slice_of<T>(t.c[PHK_Z][j], Sp, pk.slicer.negate,
                                           pk_tail, pk_iw, epk);
                 if (s < 0 || i0 + j >= a.n) continue;
-                T& kxp = v[PHK_XP][j];
-                T& kyp = v[PHK_YP][j];
-                T& kdp = v[PHK_DP][j];
-                const T kx = v[PHK_X][j], ky = v[PHK_Y][j];
-                for (int k = 0; k < pk.n_kicks; ++k) {
-                    T val = kick_value<T>(pk, k, s);
+                const T kx = t.c[PHK_X][j], ky = t.c[PHK_Y][j];
+                for (int k = 0; k < nk; ++k) {
+                    T val = a.kicks_smem
+                                ? ktab[k * Sp + s]
+                                : __ldg(reinterpret_cast<const T*>(pk.kick[k]) + s);
                     const int qd = pk.quad[k];
-                    if (qd == PHK_X) val = tmul(val, kx);
-                    else if (qd == PHK_Y) val = tmul(val, ky);
+                    if (qd == PHK_X) val = tmul<T>(val, kx);
+                    else if (qd == PHK_Y) val = tmul<T>(val, ky);
                     const int tg = pk.target[k];
-                    if (tg == PHK_XP) kxp = tadd(kxp, val);
-                    else if (tg == PHK_YP) kyp = tadd(kyp, val);
-                    else kdp = tadd(kdp, val);
+                    if (tg == PHK_XP) t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], val);
+                    else if (tg == PHK_YP) t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], val);
+                    else t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], val);
                 }
             }
         }
         // 2. element program
-        for (int o = 0; o < prog.n_ops; ++o) {
-            const phk_op& op = prog.op[o];
-#pragma unroll
-            for (int j = 0; j < VEC; ++j)
-                apply_op(op, prog, v[PHK_X][j], v[PHK_XP][j], v[PHK_Y][j],
-                         v[PHK_YP][j], v[PHK_Z][j], v[PHK_DP][j]);
-        }
+        run_program<T, VEC>(prog, t);
         // 3. slice accumulation
         if (a.has_acc) {
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
                 if (i0 + j >= a.n) continue;
-                const int s = slice_of<T>(v[PHK_Z][j], Sa, acc.slicer.negate,
+                const int s = slice_of<T>(t.c[PHK_Z][j], Sa, acc.slicer.negate,
                                           ac_tail, ac_iw, eacc);
                 if (acc.idx_out)
                     acc.idx_out[i0 + j] =
                         s >= 0 ? s
-                               : outside_index((double)v[PHK_Z][j],
+                               : outside_index((double)t.c[PHK_Z][j],
                                                acc.slicer.tail,
                                                acc.slicer.width);
                 if (s >= 0) {
-                    atomicAdd(hcnt + s, 1);
-                    atomicAdd(hsx + s, AccT(v[PHK_X][j]));
-                    atomicAdd(hsy + s, AccT(v[PHK_Y][j]));
+                    atomicAdd(my_cnt + s, 1);
+                    Hist<T>::add(my_sx + s, t.c[PHK_X][j]);
+                    Hist<T>::add(my_sy + s, t.c[PHK_Y][j]);
                 }
             }
         }
@@ -448,23 +667,30 @@ track_kernel(const __grid_constant__ phk_program prog,
         for (int q = 0; q < 6; ++q) {
             if (!((a.store_mask >> q) & 1)) continue;
             if (full) {
-                VecIO<T, VEC>::st(cp[q] + i0, v[q]);
+                VecIO<T, VEC>::st(cp[q] + i0, t.c[q]);
             } else {
 #pragma unroll
                 for (int j = 0; j < VEC; ++j)
-                    if (i0 + j < a.n) cp[q][i0 + j] = v[q][j];
+                    if (i0 + j < a.n) cp[q][i0 + j] = t.c[q][j];
             }
         }
     }
 
     if (a.has_acc) {
         __syncthreads();
+        // merge the histogram copies in a fixed order, in FP64
         const int G = gridDim.x;
         double* P = acc.partials;
         for (int s = tid; s < Sa; s += blockDim.x) {
-            P[(int64_t)s * G + blockIdx.x] = (double)hcnt[s];
-            P[(int64_t)(Sa + s) * G + blockIdx.x] = (double)hsx[s];
-            P[(int64_t)(2 * Sa + s) * G + blockIdx.x] = (double)hsy[s];
+            double c = 0.0, sx = 0.0, sy = 0.0;
+            for (int k = 0; k < a.n_hist; ++k) {
+                c += (double)hcnt[k * Sa + s];
+                sx += Hist<T>::value(hsx + k * Sa + s);
+                sy += Hist<T>::value(hsy + k * Sa + s);
+            }
+            P[(int64_t)s * G + blockIdx.x] = c;
+            P[(int64_t)(Sa + s) * G + blockIdx.x] = sx;
+            P[(int64_t)(2 * Sa + s) * G + blockIdx.x] = sy;
         }
     }
 }
@@ -473,18 +699,31 @@ track_kernel(const __grid_constant__ phk_program prog,
 // launch configuration
 // ===================================================================
 
-template <typename T, int VEC>
-static size_t smem_bytes(int Sa, int Sp) {
-    using AccT = typename AccumType<T>::type;
-    size_t b = 0;
-    if (Sa > 0) b += 2 * sizeof(AccT) * Sa + sizeof(T) * (Sa + 1) + sizeof(int) * Sa;
-    if (Sp > 0) b += sizeof(T) * (Sp + 1);
-    return b;
+template <typename T>
+struct TrackCfg {
+    static constexpr int VEC = sizeof(T) == 8 ? 2 : 4;
+};
+
+// histogram copies: one per warp while they fit in 96 KB, else one per CTA
+template <typename T>
+static int hist_copies(int Sa) {
+    if (Sa <= 0) return 1;
+    const int warps = kTrackThreads / 32;
+    return (size_t)warps * Sa * 20 <= 96 * 1024 ? warps : 1;
+}
+
+template <typename T>
+static size_t smem_for(int Sa, int Sp, int nk, int* n_hist, int* kicks_smem) {
+    size_t off[6];
+    *n_hist = hist_copies<T>(Sa);
+    *kicks_smem = (size_t)nk * Sp * sizeof(T) <= 48 * 1024;
+    return track_smem_layout<T>(Sa, Sp, *n_hist, nk, *kicks_smem, off);
 }
 
 size_t track_smem_bytes(int32_t dtype, int32_t Sa, int32_t Sp) {
-    return dtype == PHK_F64 ? smem_bytes<double, 2>(Sa, Sp)
-                            : smem_bytes<float, 4>(Sa, Sp);
+    int nh, ks;
+    return dtype == PHK_F64 ? smem_for<double>(Sa, Sp, 4, &nh, &ks)
+                            : smem_for<float>(Sa, Sp, 4, &nh, &ks);
 }
 
 // Opt the track kernel into the device's full dynamic shared memory, once
@@ -545,7 +784,8 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     static phk_accum zero_acc;
     const int Sa = acc ? acc->slicer.n_slices : 0;
     const int Sp = pk ? pk->slicer.n_slices : 0;
-    const size_t smem = smem_bytes<T, VEC>(Sa, Sp);
+    const int nk = pk ? pk->n_kicks : 0;
+    const size_t smem = smem_for<T>(Sa, Sp, nk, &a.n_hist, &a.kicks_smem);
     if (smem > (size_t)device_info().max_smem_optin)
         return set_error(PHK_ESIZE, "phk_track: %zu bytes of shared memory "
                          "needed for %d + %d slices", smem, Sa, Sp);
