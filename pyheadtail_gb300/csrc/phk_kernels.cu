@@ -414,11 +414,16 @@ __device__ __forceinline__ void run_program(const phk_program& prog,
 }
 
 // ===================================================================
-// per-slice accumulation in shared memory
-//   FP64 form: per-warp (or per-CTA) histograms of double sums
-//   FP32 form: per-warp histograms of Kahan-compensated float sums; the
-//              (sum, compensation) pair of a bin is one 64-bit word updated
-//              with a 64-bit compare-and-swap, so each update is atomic
+// per-slice accumulation in shared memory, deterministic
+//   Each warp owns a private histogram (count, sum x, sum y per slice).
+//   Lanes of a warp holding the same slice are found with match.any; they
+//   update the bin one after the other in lane order (rank steps separated
+//   by __syncwarp), so no atomics are needed and the sums do not depend on
+//   scheduling.  FP64 form: plain double sums.  FP32 form: Kahan (1965)
+//   compensated float sums, one (sum, compensation) float2 per bin.
+//   When the per-warp copies do not fit, warps share one histogram and the
+//   updates fall back to atomics (FP64 form only needs that above ~500
+//   slices; the FP32 form always fits up to PHK_MAX_SLICES / 8 warps).
 // ===================================================================
 
 template <typename T>
@@ -427,9 +432,11 @@ struct Hist;
 template <>
 struct Hist<double> {
     using Word = double;
-    static constexpr int kWordBytes = 8;
     static __device__ __forceinline__ void zero(Word* w) { *w = 0.0; }
     static __device__ __forceinline__ void add(Word* w, double v) {
+        *w = ::phk::add(*w, v);
+    }
+    static __device__ __forceinline__ void add_atomic(Word* w, double v) {
         atomicAdd(w, v);
     }
     static __device__ __forceinline__ double value(const Word* w) { return *w; }
@@ -437,30 +444,55 @@ struct Hist<double> {
 
 template <>
 struct Hist<float> {
-    using Word = unsigned long long;  // low 32 bits: sum, high: compensation
-    static constexpr int kWordBytes = 8;
-    static __device__ __forceinline__ void zero(Word* w) { *w = 0ull; }
+    using Word = float2;  // x: running sum, y: Kahan compensation
+    static __device__ __forceinline__ void zero(Word* w) {
+        *w = make_float2(0.f, 0.f);
+    }
     static __device__ __forceinline__ void add(Word* w, float v) {
-        Word old = *w, assumed;
-        do {
-            assumed = old;
-            const float s = __uint_as_float((unsigned)(assumed & 0xffffffffu));
-            const float c = __uint_as_float((unsigned)(assumed >> 32));
-            // Kahan (1965) compensated summation step
-            const float yk = v - c;
-            const float tk = s + yk;
-            const float cn = (tk - s) - yk;
-            const Word nw = (Word)__float_as_uint(tk) |
-                            ((Word)__float_as_uint(cn) << 32);
-            old = atomicCAS(w, assumed, nw);
-        } while (old != assumed);
+        float2 a = *w;
+        const float yk = v - a.y;
+        const float tk = a.x + yk;
+        a.y = (tk - a.x) - yk;
+        a.x = tk;
+        *w = a;
+    }
+    static __device__ __forceinline__ void add_atomic(Word* w, float v) {
+        atomicAdd(&w->x, v);
     }
     static __device__ __forceinline__ double value(const Word* w) {
-        const float s = __uint_as_float((unsigned)(*w & 0xffffffffu));
-        const float c = __uint_as_float((unsigned)(*w >> 32));
-        return (double)s - (double)c;
+        const float2 a = *w;
+        return (double)a.x - (double)a.y;
     }
 };
+
+// All 32 lanes of the warp must call this together; s < 0 means "no bin".
+template <typename T>
+__device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
+                                                typename Hist<T>::Word* hx,
+                                                typename Hist<T>::Word* hy,
+                                                int* hc, bool shared_hist) {
+    const unsigned full = 0xffffffffu;
+    if (shared_hist) {
+        if (s >= 0) {
+            atomicAdd(hc + s, 1);
+            Hist<T>::add_atomic(hx + s, vx);
+            Hist<T>::add_atomic(hy + s, vy);
+        }
+        return;
+    }
+    const unsigned peers = __match_any_sync(full, s);
+    const int lane = threadIdx.x & 31;
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    const int steps = __reduce_max_sync(full, (unsigned)rank) + 1;
+    if (s >= 0 && rank == 0) hc[s] += __popc(peers);
+    for (int k = 0; k < steps; ++k) {
+        if (s >= 0 && rank == k) {
+            Hist<T>::add(hx + s, vx);
+            Hist<T>::add(hy + s, vy);
+        }
+        __syncwarp();
+    }
+}
 
 // ===================================================================
 // the fused track kernel
@@ -531,8 +563,8 @@ __host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
                                                     int n_kicks, int kicks_smem,
                                                     size_t* off) {
     size_t b = 0;
-    off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x
-    off[1] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum y
+    off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x words
+    off[1] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum y words
     off[2] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // count
     off[3] = b; b = align16(b + sizeof(T) * (Sa > 0 ? Sa + 1 : 0));
     off[4] = b; b = align16(b + sizeof(T) * (Sp > 0 ? Sp + 1 : 0));
@@ -591,6 +623,7 @@ track_kernel(const __grid_constant__ phk_program prog,
         ac_iw = span > T(0) ? T(Sa) / span : T(0);
     }
     const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
+    const bool shared_hist = a.n_hist < (int)(blockDim.x >> 5);
     W* my_sx = hsx + h * Sa;
     W* my_sy = hsy + h * Sa;
     int* my_cnt = hcnt + h * Sa;
@@ -599,9 +632,12 @@ track_kernel(const __grid_constant__ phk_program prog,
 #pragma unroll
     for (int q = 0; q < 6; ++q) cp[q] = reinterpret_cast<T*>(a.c[q]);
 
-    for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+    // every warp runs whole tiles (lanes past the end carry dead particles)
+    // so that the warp-level slice accumulation sees all 32 lanes
+    const int64_t n_tiles_grid = (a.n_tiles + gridDim.x - 1) / gridDim.x;
+    for (int64_t it = 0; it < n_tiles_grid; ++it) {
+        const int64_t tile = blockIdx.x + it * gridDim.x;
         const int64_t i0 = (tile * blockDim.x + tid) * VEC;
-        if (i0 >= a.n) continue;
         const bool full = i0 + VEC <= a.n;
         Tile<T, VEC> t;
 #pragma unroll
@@ -647,20 +683,19 @@ track_kernel(const __grid_constant__ phk_program prog,
         if (a.has_acc) {
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
-                if (i0 + j >= a.n) continue;
-                const int s = slice_of<T>(t.c[PHK_Z][j], Sa, acc.slicer.negate,
-                                          ac_tail, ac_iw, eacc);
-                if (acc.idx_out)
+                const bool live = i0 + j < a.n;
+                const int s = live ? slice_of<T>(t.c[PHK_Z][j], Sa,
+                                                 acc.slicer.negate, ac_tail,
+                                                 ac_iw, eacc)
+                                   : -1;
+                if (acc.idx_out && live)
                     acc.idx_out[i0 + j] =
                         s >= 0 ? s
                                : outside_index((double)t.c[PHK_Z][j],
                                                acc.slicer.tail,
                                                acc.slicer.width);
-                if (s >= 0) {
-                    atomicAdd(my_cnt + s, 1);
-                    Hist<T>::add(my_sx + s, t.c[PHK_X][j]);
-                    Hist<T>::add(my_sy + s, t.c[PHK_Y][j]);
-                }
+                warp_accumulate<T>(s, t.c[PHK_X][j], t.c[PHK_Y][j], my_sx,
+                                   my_sy, my_cnt, shared_hist);
             }
         }
 #pragma unroll
