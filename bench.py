@@ -57,6 +57,10 @@ WORKLOADS = {
 }
 
 L2_FLUSH_BYTES = 512 << 20
+# GPU spin (cycles) queued before each timed span, so that the span's events
+# and kernels are all enqueued while the GPU is busy: the events then
+# measure device time only, not the host's launch path
+SPIN_CYCLES = 400000
 
 
 def bunch_coords(w):
@@ -260,6 +264,7 @@ def time_form(w, coords, precision, steps, warmup, flush):
     n0 = N.launch_count()
     for i in range(steps):
         flush.zero_()                   # evict L2 (outside the timed span)
+        torch.cuda._sleep(SPIN_CYCLES)
         starts[i].record()
         tg.replay(1)
         ends[i].record()
@@ -275,12 +280,15 @@ def time_form(w, coords, precision, steps, warmup, flush):
     torch.cuda.synchronize()
     kernels_per_turn = N.launch_count() - n_eager0
     del n0
-    # track kernel alone: eager turns with events around phk_track
+    # track kernel alone: eager turns with events around phk_track (the
+    # last element, the WakeField, launches it)
     beam._engine.track_events = []
     for i in range(steps):
-        flush.zero_()
-        for m in elements:
+        for m in elements[:-1]:
             m.track(beam)
+        flush.zero_()
+        torch.cuda._sleep(SPIN_CYCLES)
+        elements[-1].track(beam)
     torch.cuda.synchronize()
     evs = beam._engine.track_events
     beam._engine.track_events = None
