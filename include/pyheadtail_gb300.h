@@ -177,10 +177,12 @@ typedef struct phk_kick_set {
 } phk_kick_set;
 
 /* ---- per-slice accumulation (Slicer.slice + add_statistics for the
- *      dipole moments: slicing.py:348-381, 443-470; stats.pyx:192-253).
- * Each of the `grid` CTAs writes its per-slice count / sum x / sum y to
- * partials[q * n_slices * grid + s * grid + cta] (q = 0,1,2); use
- * phk_track_grid() for `grid` and size partials >= 3 * n_slices * grid.
+ * dipole moments: slicing.py:348-381, 443-470; stats.pyx:192-253).
+ * An accumulating phk_track runs `grid` thread-block clusters; each cluster
+ * folds its CTAs' histograms through distributed shared memory and writes
+ * its per-slice count / sum x / sum y to the partial column
+ * partials[q * n_slices * grid + s * grid + column] (q = 0,1,2).  Use
+ * phk_track_grid() for `grid`; size partials >= 3 * n_slices * grid.
  * idx_out (optional, int32[n]) receives the reference's slice index of
  * every particle (outside particles included; NaN -> INT32_MIN).        */
 typedef struct phk_accum {
@@ -236,8 +238,9 @@ int64_t phk_launch_count(void);
  * len bytes) and returns its full length. */
 int phk_last_error(char *buf, int len);
 
-/* Number of CTAs phk_track() uses for n particles of dtype with an
- * accumulation over n_slices slices (sizes the partials workspace). */
+/* Number of partial columns (thread-block clusters) an accumulating
+ * phk_track() uses for n particles of dtype over n_slices slices; sizes the
+ * partials workspace. */
 int phk_track_grid(int64_t n, int32_t dtype, int32_t n_slices);
 
 /* The fused turn kernel.  In one pass over the particles:

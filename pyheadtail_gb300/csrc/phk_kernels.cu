@@ -6,6 +6,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <cooperative_groups.h>
+
 #include <type_traits>
 
 #include "phk_device.cuh"
@@ -439,6 +441,9 @@ struct Hist<double> {
     static __device__ __forceinline__ void add_atomic(Word* w, double v) {
         atomicAdd(w, v);
     }
+    static __device__ __forceinline__ void merge(Word* dst, const Word* src) {
+        *dst = ::phk::add(*dst, *src);
+    }
     static __device__ __forceinline__ double value(const Word* w) { return *w; }
 };
 
@@ -459,9 +464,13 @@ struct Hist<float> {
     static __device__ __forceinline__ void add_atomic(Word* w, float v) {
         atomicAdd(&w->x, v);
     }
+    static __device__ __forceinline__ void merge(Word* dst, const Word* src) {
+        const float2 b = *src;
+        add(dst, b.x - b.y);
+    }
     static __device__ __forceinline__ double value(const Word* w) {
         const float2 a = *w;
-        return (double)a.x - (double)a.y;
+        return (double)(a.x - a.y);
     }
 };
 
@@ -536,6 +545,8 @@ struct TrackArgs {
     int32_t store_mask;
     int32_t n_hist;      // histogram copies per CTA (1 or warps per CTA)
     int32_t kicks_smem;  // kick tables staged in shared memory
+    int32_t cluster;     // CTAs per thread-block cluster (accumulation)
+    int32_t reserved;
 };
 
 template <typename T>
@@ -713,19 +724,48 @@ track_kernel(const __grid_constant__ phk_program prog,
 
     if (a.has_acc) {
         __syncthreads();
-        // merge the histogram copies in a fixed order, in FP64
-        const int G = gridDim.x;
+        // fold the per-warp copies into copy 0, in the storage precision
+        // (fixed order; no FP64 arithmetic in the FP32 form)
+        for (int s = tid; s < Sa; s += blockDim.x) {
+            int c = hcnt[s];
+            for (int k = 1; k < a.n_hist; ++k) {
+                c += hcnt[k * Sa + s];
+                Hist<T>::merge(hsx + s, hsx + k * Sa + s);
+                Hist<T>::merge(hsy + s, hsy + k * Sa + s);
+            }
+            hcnt[s] = c;
+        }
+        int column = blockIdx.x;
+        if (a.cluster > 1) {
+            // fold the CTAs of the thread-block cluster into its rank 0
+            // through distributed shared memory
+            namespace cg = cooperative_groups;
+            cg::cluster_group cl = cg::this_cluster();
+            cl.sync();
+            const unsigned rank = cl.block_rank();
+            if (rank == 0) {
+                for (int s = tid; s < Sa; s += blockDim.x) {
+                    int c = hcnt[s];
+                    for (unsigned r = 1; r < cl.num_blocks(); ++r) {
+                        c += *cl.map_shared_rank(hcnt + s, r);
+                        Hist<T>::merge(hsx + s, cl.map_shared_rank(hsx + s, r));
+                        Hist<T>::merge(hsy + s, cl.map_shared_rank(hsy + s, r));
+                    }
+                    hcnt[s] = c;
+                }
+            }
+            cl.sync();  // members keep their shared memory until read
+            if (rank != 0) return;
+            column = blockIdx.x / a.cluster;
+        } else {
+            __syncthreads();
+        }
+        const int G = acc.grid;
         double* P = acc.partials;
         for (int s = tid; s < Sa; s += blockDim.x) {
-            double c = 0.0, sx = 0.0, sy = 0.0;
-            for (int k = 0; k < a.n_hist; ++k) {
-                c += (double)hcnt[k * Sa + s];
-                sx += Hist<T>::value(hsx + k * Sa + s);
-                sy += Hist<T>::value(hsy + k * Sa + s);
-            }
-            P[(int64_t)s * G + blockIdx.x] = c;
-            P[(int64_t)(Sa + s) * G + blockIdx.x] = sx;
-            P[(int64_t)(2 * Sa + s) * G + blockIdx.x] = sy;
+            P[(int64_t)s * G + column] = (double)hcnt[s];
+            P[(int64_t)(Sa + s) * G + column] = Hist<T>::value(hsx + s);
+            P[(int64_t)(2 * Sa + s) * G + column] = Hist<T>::value(hsy + s);
         }
     }
 }
@@ -775,6 +815,9 @@ static void prepare_track_kernel() {
     done_for[dev] = 1;
 }
 
+// CTAs per thread-block cluster of an accumulating launch
+constexpr int kCluster = 4;
+
 template <typename T, int VEC>
 static int occupancy_blocks(size_t smem) {
     int b = 0;
@@ -785,18 +828,43 @@ static int occupancy_blocks(size_t smem) {
     return b < 1 ? 1 : b;
 }
 
+// clusters of kCluster CTAs that can be resident at once
+template <typename T, int VEC>
+static int occupancy_clusters(size_t smem) {
+    prepare_track_kernel<T, VEC>();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kCluster * device_info().sm_count, 1, 1);
+    cfg.blockDim = dim3(kTrackThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = kCluster;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, track_kernel<T, VEC>, &cfg) !=
+            cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = device_info().sm_count / kCluster;
+    }
+    return n < 1 ? 1 : n;
+}
+
+// partial columns (= clusters) of an accumulating launch over n particles
 int track_grid(int64_t n, int32_t dtype, int32_t n_slices) {
-    const DeviceInfo& d = device_info();
-    // size the grid for an accumulation with a pending kick on the same
-    // slicing (the largest shared-memory layout of a turn)
+    // size for an accumulation with a pending kick on the same slicing (the
+    // largest shared-memory layout of a turn)
     const size_t smem = track_smem_bytes(dtype, n_slices, n_slices);
     const int vec = dtype == PHK_F64 ? 2 : 4;
-    const int bps = dtype == PHK_F64 ? occupancy_blocks<double, 2>(smem)
-                                     : occupancy_blocks<float, 4>(smem);
+    const int nc = dtype == PHK_F64 ? occupancy_clusters<double, 2>(smem)
+                                    : occupancy_clusters<float, 4>(smem);
     const int64_t tiles = (n + (int64_t)kTrackThreads * vec - 1) /
                           ((int64_t)kTrackThreads * vec);
-    int64_t g = (int64_t)d.sm_count * bps;
-    if (tiles < g) g = tiles;
+    int64_t g = nc;
+    const int64_t need = (tiles + kCluster - 1) / kCluster;
+    if (need < g) g = need;
     if (g < 1) g = 1;
     return (int)g;
 }
@@ -813,6 +881,8 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     a.has_acc = acc != nullptr;
     a.load_mask = load_mask;
     a.store_mask = store_mask;
+    a.cluster = 1;
+    a.reserved = 0;
     const int64_t per_tile = (int64_t)kTrackThreads * VEC;
     a.n_tiles = (c->n + per_tile - 1) / per_tile;
     static phk_kick_set zero_pk;
@@ -824,19 +894,34 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     if (smem > (size_t)device_info().max_smem_optin)
         return set_error(PHK_ESIZE, "phk_track: %zu bytes of shared memory "
                          "needed for %d + %d slices", smem, Sa, Sp);
-    int grid;
+    prepare_track_kernel<T, VEC>();
+    cudaError_t e;
     if (acc) {
-        grid = acc->grid;
+        // one partial column per cluster of kCluster CTAs
+        a.cluster = kCluster;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)acc->grid * kCluster, 1, 1);
+        cfg.blockDim = dim3(kTrackThreads, 1, 1);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = kCluster;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, track_kernel<T, VEC>, *prog, pk ? *pk : zero_pk,
+                               *acc, a);
     } else {
         const int bps = occupancy_blocks<T, VEC>(smem);
         int64_t g = (int64_t)device_info().sm_count * bps;
         if (a.n_tiles < g) g = a.n_tiles;
-        grid = (int)(g < 1 ? 1 : g);
+        const int grid = (int)(g < 1 ? 1 : g);
+        track_kernel<T, VEC><<<grid, kTrackThreads, smem, st>>>(
+            *prog, pk ? *pk : zero_pk, zero_acc, a);
+        e = cudaGetLastError();
     }
-    prepare_track_kernel<T, VEC>();
-    track_kernel<T, VEC><<<grid, kTrackThreads, smem, st>>>(
-        *prog, pk ? *pk : zero_pk, acc ? *acc : zero_acc, a);
-    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_track launch: %s", cudaGetErrorString(e));
     count_launches(1);
@@ -911,23 +996,40 @@ __global__ void finalize_kernel(const double* __restrict__ P, int S, int G,
     const int lane = threadIdx.x & 31;
     if (warp >= S) return;
     const int s = warp;
-    double c = 0.0, sx = 0.0, sy = 0.0;
-    for (int g = lane; g < G; g += 32) {
-        c += P[(int64_t)s * G + g];
-        sx += P[(int64_t)(S + s) * G + g];
-        sy += P[(int64_t)(2 * S + s) * G + g];
+    const double* pc = P + (int64_t)s * G;
+    const double* px = P + (int64_t)(S + s) * G;
+    const double* py = P + (int64_t)(2 * S + s) * G;
+    // four independent strided partial sums per lane (loads in flight),
+    // combined in a fixed order: the result does not depend on timing
+    double c[4] = {0, 0, 0, 0}, sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0};
+    int g = lane;
+    for (; g + 96 < G; g += 128) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            c[u] += pc[g + 32 * u];
+            sx[u] += px[g + 32 * u];
+            sy[u] += py[g + 32 * u];
+        }
     }
+    for (; g < G; g += 32) {
+        c[0] += pc[g];
+        sx[0] += px[g];
+        sy[0] += py[g];
+    }
+    double tc = (c[0] + c[1]) + (c[2] + c[3]);
+    double tx = (sx[0] + sx[1]) + (sx[2] + sx[3]);
+    double ty = (sy[0] + sy[1]) + (sy[2] + sy[3]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        c += __shfl_xor_sync(0xffffffffu, c, o);
-        sx += __shfl_xor_sync(0xffffffffu, sx, o);
-        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        tc += __shfl_xor_sync(0xffffffffu, tc, o);
+        tx += __shfl_xor_sync(0xffffffffu, tx, o);
+        ty += __shfl_xor_sync(0xffffffffu, ty, o);
     }
     if (lane != 0) return;
-    const int32_t n = (int32_t)c;
+    const int32_t n = (int32_t)tc;
     // stats.pyx:251-253: divide non-empty slices by their count
-    const double mx = n ? dvd(sx, (double)n) : 0.0;
-    const double my = n ? dvd(sy, (double)n) : 0.0;
+    const double mx = n ? dvd(tx, (double)n) : 0.0;
+    const double my = n ? dvd(ty, (double)n) : 0.0;
     if (counts) counts[s] = n;
     if (mean_x) mean_x[s] = mx;
     if (mean_y) mean_y[s] = my;
@@ -979,8 +1081,15 @@ __global__ void wake_conv_kernel(const __grid_constant__ phk_wake_set w) {
         const int slot = ((w.head - a) % w.ring_len + w.ring_len) % w.ring_len;
         const double* m = w.moments + ((int64_t)slot * 3 + kk.source) * S;
         const double* v = kk.table + (int64_t)a * L2 + i + S - 1;
-        double part = 0.0;
-        for (int j = lane; j < S; j += 32) part = fma(m[j], v[-j], part);
+        double p0 = 0.0, p1 = 0.0;
+        int j = lane;
+#pragma unroll 4
+        for (; j + 32 < S; j += 64) {
+            p0 = fma(m[j], v[-j], p0);
+            p1 = fma(m[j + 32], v[-j - 32], p1);
+        }
+        if (j < S) p0 = fma(m[j], v[-j], p0);
+        double part = p0 + p1;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             part += __shfl_xor_sync(0xffffffffu, part, o);
