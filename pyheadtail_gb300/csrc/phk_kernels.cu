@@ -475,12 +475,18 @@ struct Hist<float> {
 };
 
 // All 32 lanes of the warp must call this together; s < 0 means "no bin".
+// Lanes of a warp that hold the same slice are serialised by bids: in each
+// round every pending lane bids atomicMax(tag[s], epoch << 5 | lane) on the
+// warp's private tag array; the standing bid (the highest pending lane of
+// that slice) updates the bin with plain loads and stores.  A bin is thus
+// always updated in descending lane order: the sums are deterministic.
 template <typename T>
 __device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
                                                 typename Hist<T>::Word* hx,
                                                 typename Hist<T>::Word* hy,
-                                                int* hc, bool shared_hist) {
-    const unsigned full = 0xffffffffu;
+                                                int* hc, int* tag,
+                                                unsigned& epoch,
+                                                bool shared_hist) {
     if (shared_hist) {
         if (s >= 0) {
             atomicAdd(hc + s, 1);
@@ -489,15 +495,18 @@ __device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
         }
         return;
     }
-    const unsigned peers = __match_any_sync(full, s);
     const int lane = threadIdx.x & 31;
-    const int rank = __popc(peers & ((1u << lane) - 1u));
-    const int steps = __reduce_max_sync(full, (unsigned)rank) + 1;
-    if (s >= 0 && rank == 0) hc[s] += __popc(peers);
-    for (int k = 0; k < steps; ++k) {
-        if (s >= 0 && rank == k) {
+    bool pending = s >= 0;
+    while (__any_sync(0xffffffffu, pending)) {
+        ++epoch;
+        const int bid = (int)((epoch << 5) | (unsigned)lane);
+        if (pending) atomicMax(tag + s, bid);
+        __syncwarp();
+        if (pending && tag[s] == bid) {
+            hc[s] += 1;
             Hist<T>::add(hx + s, vx);
             Hist<T>::add(hy + s, vy);
+            pending = false;
         }
         __syncwarp();
     }
@@ -566,7 +575,7 @@ __device__ __forceinline__ float tmul<float>(float a, float b) { return a * b; }
 //   histogram words  [3][n_hist][Sa]   (sum x, sum y as Hist<T>::Word; count
 //                                       as int in the third region)
 //   accumulation edges [Sa + 1] T, pending-kick edges [Sp + 1] T,
-//   kick tables [n_kicks][Sp] T (when staged)
+//   kick tables [n_kicks][Sp] T (when staged), bid tags [n_hist][Sa] int
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
 template <typename T>
@@ -580,6 +589,7 @@ __host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
     off[3] = b; b = align16(b + sizeof(T) * (Sa > 0 ? Sa + 1 : 0));
     off[4] = b; b = align16(b + sizeof(T) * (Sp > 0 ? Sp + 1 : 0));
     off[5] = b; b = align16(b + (kicks_smem ? sizeof(T) * (size_t)n_kicks * Sp : 0));
+    off[6] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // bid tags
     return b;
 }
 
@@ -593,7 +603,7 @@ track_kernel(const __grid_constant__ phk_program prog,
     const int Sa = a.has_acc ? acc.slicer.n_slices : 0;
     const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
     const int nk = a.has_pk ? pk.n_kicks : 0;
-    size_t off[6];
+    size_t off[7];
     track_smem_layout<T>(Sa, Sp, a.n_hist, nk, a.kicks_smem, off);
     W* hsx = reinterpret_cast<W*>(smem + off[0]);
     W* hsy = reinterpret_cast<W*>(smem + off[1]);
@@ -601,13 +611,15 @@ track_kernel(const __grid_constant__ phk_program prog,
     T* eacc = reinterpret_cast<T*>(smem + off[3]);
     T* epk = reinterpret_cast<T*>(smem + off[4]);
     T* ktab = reinterpret_cast<T*>(smem + off[5]);
+    int* htag = reinterpret_cast<int*>(smem + off[6]);
 
     const int tid = threadIdx.x;
     if (a.has_acc) {
         const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
         for (int i = tid; i <= Sa; i += blockDim.x) eacc[i] = e[i];
         for (int i = tid; i < a.n_hist * Sa; i += blockDim.x) {
-            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i); hcnt[i] = 0;
+            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
+            hcnt[i] = 0; htag[i] = 0;
         }
     }
     if (a.has_pk) {
@@ -638,6 +650,8 @@ track_kernel(const __grid_constant__ phk_program prog,
     W* my_sx = hsx + h * Sa;
     W* my_sy = hsy + h * Sa;
     int* my_cnt = hcnt + h * Sa;
+    int* my_tag = htag + h * Sa;
+    unsigned epoch = 0;
 
     T* cp[6];
 #pragma unroll
@@ -706,7 +720,7 @@ track_kernel(const __grid_constant__ phk_program prog,
                                                acc.slicer.tail,
                                                acc.slicer.width);
                 warp_accumulate<T>(s, t.c[PHK_X][j], t.c[PHK_Y][j], my_sx,
-                                   my_sy, my_cnt, shared_hist);
+                                   my_sy, my_cnt, my_tag, epoch, shared_hist);
             }
         }
 #pragma unroll
@@ -784,12 +798,12 @@ template <typename T>
 static int hist_copies(int Sa) {
     if (Sa <= 0) return 1;
     const int warps = kTrackThreads / 32;
-    return (size_t)warps * Sa * 20 <= 96 * 1024 ? warps : 1;
+    return (size_t)warps * Sa * 24 <= 112 * 1024 ? warps : 1;
 }
 
 template <typename T>
 static size_t smem_for(int Sa, int Sp, int nk, int* n_hist, int* kicks_smem) {
-    size_t off[6];
+    size_t off[7];
     *n_hist = hist_copies<T>(Sa);
     *kicks_smem = (size_t)nk * Sp * sizeof(T) <= 48 * 1024;
     return track_smem_layout<T>(Sa, Sp, *n_hist, nk, *kicks_smem, off);
