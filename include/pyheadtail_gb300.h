@@ -114,6 +114,9 @@ typedef struct phk_slicer {
  *  TRANSVERSE, detuned:     p[0..7]  = I00 I01 I10 I11 I22 I23 I32 I33
  *                           p[8..15] = J00 J01 J10 J11 J22 J23 J32 J33
  *                           p[20], p[21] = dQ_x, dQ_y;  p[22] = 2*pi
+ *                           p[23..25] = phi0_x = dQ_x*2pi, sin, cos of it
+ *                           p[26..28] = phi0_y, sin, cos (base of the
+ *                           angle-addition evaluation of sin/cos(phase))
  *                           ij_mask bit b set <=> entry b of (I..., J...) != 0
  *                           detuners det[det_begin .. det_begin+det_count)
  *  TRANSVERSE, either:      p[16..19] = D_x_s0 D_x_s1 D_y_s0 D_y_s1
@@ -121,9 +124,10 @@ typedef struct phk_slicer {
  *  RF_KICK:      p[0] = harmonic, p[1] = 2*pi, p[2] = circumference,
  *                p[3] = phi_offset, p[4] = _phi_lock, p[5] = |q| V / (beta c),
  *                p[6] = p0 before, p[7] = p_increment, p[8] = p0 after,
- *                p[9] = D_x, p[10] = D_y
+ *                p[9] = D_x, p[10] = D_y, p[11] = 1/circumference,
+ *                p[12] = 1/(p0 after)   (reciprocals rounded to nearest)
  *  LINEAR_LONG:  p[0] = cos(2 pi Q_s), p[1] = sin(2 pi Q_s), p[2] = longfac,
- *                p[3] = D_x, p[4] = D_y
+ *                p[3] = D_x, p[4] = D_y, p[5] = 1/longfac
  *  SCALE_TRANS:  p[0] = sqrt(betagamma_old / betagamma_new)
  */
 typedef struct phk_op {
@@ -133,7 +137,7 @@ typedef struct phk_op {
     int32_t det_count;
     int32_t ij_mask;
     int32_t reserved;
-    double p[24];
+    double p[32];
 } phk_op;
 
 /* detuners: ChromaticitySegment.detune (trackers/detuners.py:64-98) and
@@ -143,7 +147,8 @@ typedef struct phk_op {
  *          factors of dp (the reference's order > 3 polyval path prepends
  *          one zero coefficient per call, detuners.py:95-97).
  *  AMPLITUDE: c[0..9] = dapp_x, dapp_y, dapp_xy, dapp_yx,
- *             (1+ax^2)/bx, 2 ax, bx, (1+ay^2)/by, 2 ay, by;  c[10] = p0    */
+ *             (1+ax^2)/bx, 2 ax, bx, (1+ay^2)/by, 2 ay, by;  c[10] = p0,
+ *             c[11] = 1/p0 (rounded to nearest)                            */
 #define PHK_DET_CHROMA 1
 #define PHK_DET_AMPLITUDE 2
 typedef struct phk_detuner {

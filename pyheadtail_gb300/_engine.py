@@ -150,7 +150,7 @@ def split_ff(v):
 class Op(object):
     """One element step of a pending program.  ``p`` holds the FP64
     parameters in the layout of include/pyheadtail_gb300.h; ``pf`` (FP32
-    form) the float parameters packed into the same 192 bytes."""
+    form) the float parameters packed into the same 256 bytes."""
 
     def __init__(self, kind, flags=0, p=None, pf=None, detuners=(),
                  ij_mask=0):
@@ -170,10 +170,10 @@ class Op(object):
             for k, v in self.p.items():
                 st.p[k] = v
         else:
-            buf = np.zeros(48, dtype=np.float32)
+            buf = np.zeros(64, dtype=np.float32)
             for k, v in self.pf.items():
                 buf[k] = v
-            ctypes.memmove(ctypes.addressof(st.p), buf.ctypes.data, 192)
+            ctypes.memmove(ctypes.addressof(st.p), buf.ctypes.data, 256)
 
 
 class DetunerPack(object):

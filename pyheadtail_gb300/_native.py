@@ -48,7 +48,7 @@ class Op(ctypes.Structure):
     _fields_ = [('kind', ctypes.c_int32), ('flags', ctypes.c_int32),
                 ('det_begin', ctypes.c_int32), ('det_count', ctypes.c_int32),
                 ('ij_mask', ctypes.c_int32), ('reserved', ctypes.c_int32),
-                ('p', ctypes.c_double * 24)]
+                ('p', ctypes.c_double * 32)]
 
 
 class Detuner(ctypes.Structure):

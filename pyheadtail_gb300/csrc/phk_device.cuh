@@ -19,6 +19,57 @@ __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, 
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
 
+// Correctly rounded a / b for a divisor b known on the host, with
+// y = RN(1/b) also from the host: q = RN(a y) is within one ulp of a/b, the
+// remainder r = a - b q is exact through an FMA, and RN(q + r y) is the
+// correctly rounded quotient (Markstein's theorem, IBM J. Res. Dev. 34,
+// 1990; the basis of IA-64 division).  The theorem needs operands and
+// quotient away from underflow and overflow; outside a safe exponent window
+// the IEEE division is used.  Three FP64 instructions instead of a full
+// division on GB300's slow FP64 pipe.
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+    const double q = mul(a, y);
+    const int ea = (__double2hiint(a) >> 20) & 0x7ff;
+    const int eq = (__double2hiint(q) >> 20) & 0x7ff;
+    if (ea > 64 && ea < 1984 && eq > 64 && eq < 1984) {
+        const double r = fma(-b, q, a);
+        return fma(r, y, q);
+    }
+    return dvd(a, b);
+}
+
+// sin and cos of phi = phi0 + d for a base phi0 whose sine s0 and cosine c0
+// are known (host, correctly rounded): angle addition with the Maclaurin
+// series of sin d (to d^11) and cos d (to d^12), whose truncation errors
+// are below 3e-18 and 5e-20 for |d| <= 1/4.  d = phi - phi0 is exact when
+// phi and phi0 are within a factor two (Sterbenz).  Larger |d| falls back
+// to the library sincos.
+__device__ __forceinline__ void sincos_about(double phi, double phi0,
+                                             double s0, double c0, double* s,
+                                             double* c) {
+    const double d = phi - phi0;
+    if (!(fabs(d) <= 0.25)) {
+        sincos(phi, s, c);
+        return;
+    }
+    const double d2 = d * d;
+    // sin d = d + d^3 (-1/3! + d^2 (1/5! + d^2 (-1/7! + d^2 (1/9! - d^2/11!))))
+    double ps = fma(d2, -1.0 / 39916800.0, 1.0 / 362880.0);
+    ps = fma(d2, ps, -1.0 / 5040.0);
+    ps = fma(d2, ps, 1.0 / 120.0);
+    ps = fma(d2, ps, -1.0 / 6.0);
+    const double sd = fma(d * d2, ps, d);
+    // cos d = 1 + d^2 (-1/2! + d^2 (1/4! + ... + d^2 / 12!))
+    double pc = fma(d2, 1.0 / 479001600.0, -1.0 / 3628800.0);
+    pc = fma(d2, pc, 1.0 / 40320.0);
+    pc = fma(d2, pc, -1.0 / 720.0);
+    pc = fma(d2, pc, 1.0 / 24.0);
+    pc = fma(d2, pc, -0.5);
+    const double cd = fma(d2, pc, 1.0);
+    *s = fma(s0, cd, c0 * sd);
+    *c = fma(c0, cd, -(s0 * sd));
+}
+
 // ---------------------------------------------------------------- binning
 // Exact reference slice index from the host-built lower-edge table
 // e[0..S]: inside iff e[0] <= z < e[S], index k with e[k] <= z < e[k+1].
@@ -36,6 +87,48 @@ __device__ __forceinline__ int slice_of(T z, int S, int negate, T est_tail,
     return k;
 }
 
+// Order-preserving 64-bit integer key of a double (sign-magnitude to two's
+// complement): a < b  <=>  key(a) < key(b) for non-NaN doubles.  NaN keys
+// fall beyond the keys of +-inf, i.e. outside any finite slicing range.
+__device__ __forceinline__ long long order_key(double v) {
+    const long long b = __double_as_longlong(v);
+    return b >= 0 ? b : (long long)((unsigned long long)b ^ 0x7fffffffffffffffull);
+}
+
+__device__ __forceinline__ double key_to_double(long long k) {
+    return __longlong_as_double(
+        k >= 0 ? k : (long long)((unsigned long long)k ^ 0x7fffffffffffffffull));
+}
+
+// A float close to the double v (20 mantissa bits) built from v's high
+// word with integer operations only; magnitudes outside the normal float
+// range map to 0 or +-inf.  Only seeds the exact search below.
+__device__ __forceinline__ float approx_float(double v) {
+    const unsigned hi = (unsigned)__double2hiint(v);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
+    unsigned bits;
+    if (e <= 0) bits = sign;
+    else if (e >= 255) bits = sign | 0x7f800000u;
+    else bits = sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3);
+    return __uint_as_float(bits);
+}
+
+// FP64 slice index without FP64 arithmetic: ek[] holds order_key() of the
+// exact edge table; the estimate uses FP32 (tail_f, inv_w_f).
+__device__ __forceinline__ int slice_of_keys(double z, int S, int negate,
+                                             float tail_f, float inv_w_f,
+                                             const long long* __restrict__ ek) {
+    const double zz = negate ? -z : z;
+    const long long kz = order_key(zz);
+    if (kz < ek[0] || kz >= ek[S]) return -1;
+    int k = (int)((approx_float(zz) - tail_f) * inv_w_f);
+    k = k < 0 ? 0 : (k > S - 1 ? S - 1 : k);
+    while (kz < ek[k]) --k;
+    while (kz >= ek[k + 1]) ++k;
+    return k;
+}
+
 // Reference index int32(floor((z - tail)/width)) for particles outside the
 // cuts (rare): IEEE division, NaN and out-of-range map to INT32_MIN as the
 // x86 conversion of numpy's astype(int32) does.
@@ -46,12 +139,38 @@ __device__ __forceinline__ int32_t outside_index(double z, double tail,
     return (int32_t)q;
 }
 
+// --------------------------------------------------- FP32 sin/cos of 2 pi f
+// sin and cos of 2*pi*f for |f| <= 1/2 turn: quadrant q = rint(4 f) and the
+// exact remainder r = f - q/4 in [-1/8, 1/8] turn, theta = 2 pi r, then the
+// Maclaurin series of sin (to theta^9) and cos (to theta^8); truncation
+// error below 2e-9 and 2.5e-8 on |theta| <= pi/4.  The quadrant rotates
+// (s, c) by q * 90 degrees.  About 20 FP32 instructions.
+__device__ __forceinline__ void sincos_2pi(float f, float* s, float* c) {
+    const float q = rintf(4.0f * f);
+    const float r = fmaf(-0.25f, q, f);
+    const float th = 6.28318530717958647692f * r;
+    const float t2 = th * th;
+    float ps = fmaf(t2, 2.7557319224e-6f, -1.9841269841e-4f);   //  1/9!, -1/7!
+    ps = fmaf(t2, ps, 8.3333333333e-3f);                         //  1/5!
+    ps = fmaf(t2, ps, -1.6666666667e-1f);                        // -1/3!
+    const float sn = fmaf(th * t2, ps, th);
+    float pc = fmaf(t2, 2.4801587302e-5f, -1.3888888889e-3f);    //  1/8!, -1/6!
+    pc = fmaf(t2, pc, 4.1666666667e-2f);                         //  1/4!
+    pc = fmaf(t2, pc, -0.5f);                                    // -1/2!
+    const float cs = fmaf(t2, pc, 1.0f);
+    const int k = (int)q & 3;
+    const float a = (k & 1) ? cs : sn;
+    const float b = (k & 1) ? sn : cs;
+    *s = (k & 2) ? -a : a;
+    *c = ((k + 1) & 2) ? -b : b;
+}
+
 // ------------------------------------------------------- float-float phase
 // sin and cos of 2*pi*(hi + lo + d) for a phase given in turns as the
 // unevaluated sum of a float-float base (hi, lo) and a small float d.
 // The integer number of turns is removed exactly (Knuth two-sum, then
 // t - rint(t) is exact), the remaining fraction f + g is split into a float
-// f and its residual g; sincospif(2f) is corrected to first order in g.
+// f and its residual g; sin/cos(2 pi f) is corrected to first order in g.
 // The phase argument thus carries ~2^-46 turns of precision on the FP32
 // pipes (GB300's FP64 pipe runs at a small fraction of the FP32 rate).
 __device__ __forceinline__ void sincos_turns(float hi, float lo, float d,
@@ -64,7 +183,7 @@ __device__ __forceinline__ void sincos_turns(float hi, float lo, float d,
     const float f = r + err;
     const float g = (r - f) + err;
     float sp, cp;
-    sincospif(2.0f * f, &sp, &cp);
+    sincos_2pi(f, &sp, &cp);
     const float dl = 6.28318530717958647692f * g;
     *s = fmaf(dl, cp, sp);
     *c = fmaf(-dl, sp, cp);

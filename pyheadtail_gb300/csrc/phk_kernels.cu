@@ -107,17 +107,19 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
             const double ax = dt.c[0], ay = dt.c[1], axy = dt.c[2], ayx = dt.c[3];
             const double c1x = dt.c[4], tax = dt.c[5], bx = dt.c[6];
             const double c1y = dt.c[7], tay = dt.c[8], by = dt.c[9];
-            const double p0 = dt.c[10];
+            const double p0 = dt.c[10], ip0 = dt.c[11];
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
                 const double Jx = amp_action(c1x, tax, bx, x[j], xp[j]);
                 const double Jy = amp_action(c1y, tay, by, y[j], yp[j]);
-                phx[j] = add(phx[j], dvd(add(mul(ax, Jx), mul(axy, Jy)), p0));
-                phy[j] = add(phy[j], dvd(add(mul(ay, Jy), mul(ayx, Jx)), p0));
+                phx[j] = add(phx[j], div_by(add(mul(ax, Jx), mul(axy, Jy)), p0, ip0));
+                phy[j] = add(phy[j], div_by(add(mul(ay, Jy), mul(ayx, Jx)), p0, ip0));
             }
         }
     }
     const double twopi = p[22];
+    const double phx0 = p[23], sx0 = p[24], cx0 = p[25];
+    const double phy0 = p[26], sy0 = p[27], cy0 = p[28];
     const int m = op.ij_mask;
     double I[8], J[8];
     bool hI[8], hJ[8];
@@ -129,8 +131,8 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
         double sx, cx, sy, cy;
-        sincos(mul(phx[j], twopi), &sx, &cx);
-        sincos(mul(phy[j], twopi), &sy, &cy);
+        sincos_about(mul(phx[j], twopi), phx0, sx0, cx0, &sx, &cx);
+        sincos_about(mul(phy[j], twopi), phy0, sy0, cy0, &sy, &cy);
         const double M00 = ij_term(I[0], J[0], hI[0], hJ[0], cx, sx);
         const double M01 = ij_term(I[1], J[1], hI[1], hJ[1], cx, sx);
         const double M10 = ij_term(I[2], J[2], hI[2], hJ[2], cx, sx);
@@ -175,7 +177,7 @@ __device__ __forceinline__ void op_rfkick(const phk_op& op,
     const int f = op.flags;
     const double h = p[0], twopi = p[1], C = p[2], off = p[3], lock = p[4];
     const double A = p[5], p0o = p[6], pinc = p[7], p0n = p[8];
-    const double Dx = p[9], Dy = p[10];
+    const double Dx = p[9], Dy = p[10], iC = p[11], ip0n = p[12];
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
         double& dp = t.c[PHK_DP][j];
@@ -183,12 +185,12 @@ __device__ __forceinline__ void op_rfkick(const phk_op& op,
             t.c[PHK_X][j] = sub(t.c[PHK_X][j], mul(Dx, dp));
             t.c[PHK_Y][j] = sub(t.c[PHK_Y][j], mul(Dy, dp));
         }
-        double phi = mul(h, dvd(mul(twopi, t.c[PHK_Z][j]), C));
+        double phi = mul(h, div_by(mul(twopi, t.c[PHK_Z][j]), C, iC));
         if (f & PHK_FLAG_PHI_OFFSET) phi = add(phi, off);
         if (f & PHK_FLAG_PHI_LOCK) phi = add(phi, lock);
         double s = mul(A, sin(phi));
         if (f & PHK_FLAG_P_INC) s = sub(s, pinc);
-        dp = dvd(add(mul(dp, p0o), s), p0n);
+        dp = div_by(add(mul(dp, p0o), s), p0n, ip0n);
         if (f & PHK_FLAG_DISPERSION) {
             t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
             t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
@@ -201,6 +203,7 @@ __device__ __forceinline__ void op_linear_long(const phk_op& op,
                                                Tile<double, VEC>& t) {
     const double* p = op.p;
     const double cs = p[0], sn = p[1], lf = p[2], Dx = p[3], Dy = p[4];
+    const double ilf = p[5];
     const bool disp = op.flags & PHK_FLAG_DISPERSION;
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
@@ -212,7 +215,7 @@ __device__ __forceinline__ void op_linear_long(const phk_op& op,
         }
         const double z0 = z, dp0 = dp;
         z = sub(mul(z0, cs), mul(mul(lf, dp0), sn));
-        dp = add(mul(dp0, cs), mul(dvd(z0, lf), sn));
+        dp = add(mul(dp0, cs), mul(div_by(z0, lf, ilf), sn));
         if (disp) {
             t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
             t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
@@ -593,6 +596,57 @@ __host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
     return b;
 }
 
+// Exact slice lookup against a staged edge table.  FP32: the float edges
+// themselves.  FP64: order-preserving int64 keys of the edges, so that the
+// lookup needs no FP64 instruction (the first estimate is FP32).
+template <typename T>
+__device__ __forceinline__ void stage_edge(T* dst, int i, T e);
+template <>
+__device__ __forceinline__ void stage_edge<float>(float* dst, int i, float e) {
+    dst[i] = e;
+}
+template <>
+__device__ __forceinline__ void stage_edge<double>(double* dst, int i,
+                                                   double e) {
+    reinterpret_cast<long long*>(dst)[i] = order_key(e);
+}
+
+template <typename T>
+struct Bins;
+template <>
+struct Bins<float> {
+    const float* e;
+    int S, neg;
+    float tail, iw;
+    __device__ __forceinline__ void init(const float* edges, int n, int negate) {
+        e = edges; S = n; neg = negate;
+        tail = e[0];
+        const float span = e[S] - e[0];
+        iw = span > 0.f ? (float)S / span : 0.f;
+    }
+    __device__ __forceinline__ int index(float z) const {
+        return slice_of<float>(z, S, neg, tail, iw, e);
+    }
+};
+template <>
+struct Bins<double> {
+    const long long* k;
+    int S, neg;
+    float tail, iw;
+    __device__ __forceinline__ void init(const double* edges, int n, int negate) {
+        k = reinterpret_cast<const long long*>(edges); S = n; neg = negate;
+        // undo the key map for the two end edges (keys of finite doubles)
+        const float lo = approx_float(key_to_double(k[0]));
+        const float hi = approx_float(key_to_double(k[S]));
+        tail = lo;
+        const float span = hi - lo;
+        iw = span > 0.f ? (float)S / span : 0.f;
+    }
+    __device__ __forceinline__ int index(double z) const {
+        return slice_of_keys(z, S, neg, tail, iw, k);
+    }
+};
+
 template <typename T, int VEC>
 __global__ void __launch_bounds__(kTrackThreads)
 track_kernel(const __grid_constant__ phk_program prog,
@@ -616,7 +670,7 @@ track_kernel(const __grid_constant__ phk_program prog,
     const int tid = threadIdx.x;
     if (a.has_acc) {
         const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
-        for (int i = tid; i <= Sa; i += blockDim.x) eacc[i] = e[i];
+        for (int i = tid; i <= Sa; i += blockDim.x) stage_edge<T>(eacc, i, e[i]);
         for (int i = tid; i < a.n_hist * Sa; i += blockDim.x) {
             Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
             hcnt[i] = 0; htag[i] = 0;
@@ -624,7 +678,7 @@ track_kernel(const __grid_constant__ phk_program prog,
     }
     if (a.has_pk) {
         const T* e = reinterpret_cast<const T*>(pk.slicer.edges);
-        for (int i = tid; i <= Sp; i += blockDim.x) epk[i] = e[i];
+        for (int i = tid; i <= Sp; i += blockDim.x) stage_edge<T>(epk, i, e[i]);
         if (a.kicks_smem)
             for (int i = tid; i < nk * Sp; i += blockDim.x) {
                 const int k = i / Sp;
@@ -634,17 +688,9 @@ track_kernel(const __grid_constant__ phk_program prog,
     __syncthreads();
 
     // first-estimate parameters of the two bin searches, from the tables
-    T pk_tail = T(0), pk_iw = T(0), ac_tail = T(0), ac_iw = T(0);
-    if (a.has_pk) {
-        pk_tail = epk[0];
-        const T span = epk[Sp] - epk[0];
-        pk_iw = span > T(0) ? T(Sp) / span : T(0);
-    }
-    if (a.has_acc) {
-        ac_tail = eacc[0];
-        const T span = eacc[Sa] - eacc[0];
-        ac_iw = span > T(0) ? T(Sa) / span : T(0);
-    }
+    Bins<T> bpk, bac;
+    if (a.has_pk) bpk.init(epk, Sp, pk.slicer.negate);
+    if (a.has_acc) bac.init(eacc, Sa, acc.slicer.negate);
     const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
     const bool shared_hist = a.n_hist < (int)(blockDim.x >> 5);
     W* my_sx = hsx + h * Sa;
@@ -684,8 +730,7 @@ track_kernel(const __grid_constant__ phk_program prog,
         if (a.has_pk) {
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
-                const int s = slice_of<T>(t.c[PHK_Z][j], Sp, pk.slicer.negate,
-                                          pk_tail, pk_iw, epk);
+                const int s = bpk.index(t.c[PHK_Z][j]);
                 if (s < 0 || i0 + j >= a.n) continue;
                 const T kx = t.c[PHK_X][j], ky = t.c[PHK_Y][j];
                 for (int k = 0; k < nk; ++k) {
@@ -709,10 +754,7 @@ track_kernel(const __grid_constant__ phk_program prog,
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
                 const bool live = i0 + j < a.n;
-                const int s = live ? slice_of<T>(t.c[PHK_Z][j], Sa,
-                                                 acc.slicer.negate, ac_tail,
-                                                 ac_iw, eacc)
-                                   : -1;
+                const int s = live ? bac.index(t.c[PHK_Z][j]) : -1;
                 if (acc.idx_out && live)
                     acc.idx_out[i0 + j] =
                         s >= 0 ? s

@@ -89,7 +89,7 @@ class AmplitudeDetuningSegment(SegmentDetuner):
         c1y = (1 + ay**2) / by
         p0 = beam.p0
         vals = [self.dapp_x, self.dapp_y, self.dapp_xy, self.dapp_yx,
-                c1x, 2 * ax, bx, c1y, 2 * ay, by, p0]
+                c1x, 2 * ax, bx, c1y, 2 * ay, by, p0, 1. / p0]
         c = {i: float(v) for i, v in enumerate(vals)}
         cf = {0: np.float32(self.dapp_x / p0), 1: np.float32(self.dapp_y / p0),
               2: np.float32(self.dapp_xy / p0),

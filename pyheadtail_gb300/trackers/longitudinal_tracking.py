@@ -106,7 +106,8 @@ class Kick(LongitudinalMap):
              2: float(self.circumference), 3: float(self.phi_offset),
              4: float(self._phi_lock), 5: float(amplitude), 6: float(p0_old),
              7: float(self.p_increment), 8: float(p0_new),
-             9: float(self.D_x), 10: float(self.D_y)}
+             9: float(self.D_x), 10: float(self.D_y),
+             11: 1. / float(self.circumference), 12: 1. / float(p0_new)}
         # precision form: phase in turns = z h / C + (offset + lock) / 2 pi
         turns_per_m = np.float64(self.harmonic) / self.circumference
         off = (self.phi_offset + self._phi_lock) / (2 * np.pi)
@@ -299,7 +300,7 @@ class LinearMap(LongitudinalOneTurnMap):
         # D = 0 makes the reference's dispersion passes (:731-741) no-ops
         flags = N.FLAG_DISPERSION if (self.D_x or self.D_y) else 0
         p = {0: float(cosdQ_s), 1: float(sindQ_s), 2: float(longfac),
-             3: float(self.D_x), 4: float(self.D_y)}
+             3: float(self.D_x), 4: float(self.D_y), 5: 1. / float(longfac)}
         pf = {0: np.float32(cosdQ_s), 1: np.float32(sindQ_s),
               2: np.float32(longfac), 3: np.float32(1. / longfac),
               4: np.float32(self.D_x), 5: np.float32(self.D_y)}

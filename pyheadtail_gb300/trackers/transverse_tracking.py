@@ -94,6 +94,12 @@ class TransverseSegmentMap(Element):
             mask |= (I[a, b] != 0) << i
             mask |= (J[a, b] != 0) << (8 + i)
         p[20], p[21], p[22] = float(self.dQ_x), float(self.dQ_y), 2. * np.pi
+        # base of the angle-addition sin/cos: the undetuned phase advance,
+        # rounded exactly as the reference rounds dQ * 2 pi, and its sin/cos
+        for k, q in ((23, self.dQ_x), (26, self.dQ_y)):
+            phi0 = q * (2. * np.pi)
+            p[k], p[k + 1], p[k + 2] = (float(phi0), float(np.sin(phi0)),
+                                        float(np.cos(phi0)))
         # precision form: phase in turns, integer part removed exactly
         for k, q in ((16, self.dQ_x), (18, self.dQ_y)):
             frac = float(q) - np.floor(float(q))

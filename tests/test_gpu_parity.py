@@ -248,3 +248,49 @@ def test_full_size_binning_bit_exact(lib, n, S):
                        torch.zeros_like(sums))
     assert float((mean - ss.mean_x).abs().max()) <= 1e-12 * float(
         mean.abs().max())
+
+
+@pytest.mark.parametrize('name', ['linear_map', 'transverse_linear'])
+def test_fixtures_without_transcendentals_are_bit_exact(lib, name):
+    """Maps whose per-particle arithmetic is only +, -, *, / in the
+    reference's order reproduce the reference bit for bit (the FP64 kernel
+    rounds every operation separately, divisions included)."""
+    import gpu_cases as G
+    ref = load(os.path.join(GOLDEN, name + '.npz'))
+    spec = json.loads(str(ref['spec']))
+    beam = G.make_beam(spec['beam'], {k: ref['init_' + k] for k in COORDS})
+    rec = G.run(spec, beam)
+    t = spec['n_turns'] - 1
+    for k in COORDS:
+        np.testing.assert_array_equal(rec['t%d_%s' % (t, k)],
+                                      ref['t%d_%s' % (t, k)], err_msg=k)
+
+
+def test_division_by_host_constants_is_correctly_rounded(lib):
+    """z / longfac in LinearMap runs the three-instruction division by a
+    host reciprocal; compare 30 divisors x 131072 log-uniform dividends of
+    both signs (3.9e6 quotients) with NumPy's IEEE division bit for bit."""
+    import cases as C
+    import gpu_cases as G
+    from oracle import turn_loop as T
+    rng = np.random.RandomState(42)
+    n = 131072
+    mag = 10.0 ** rng.uniform(-250, 250, n)
+    z = mag * np.where(rng.rand(n) < 0.5, -1., 1.)
+    dp = rng.normal(0, 1e-3, n)
+    for i in range(30):
+        Qs = 10.0 ** rng.uniform(-3, -0.5)
+        alpha = C.GAMMA**-2 + 10.0 ** rng.uniform(-5, -1)
+        coords = {k: np.zeros(n) for k in COORDS}
+        coords['z'] = z
+        coords['dp'] = dp
+        beam = G.make_beam(C.beam_params(n, 0), coords)
+        spec = dict(beam=C.beam_params(n, 0), n_turns=1,
+                    elements=[C.linear_map(Q_s=Qs, alpha=alpha)])
+        G.run(spec, beam)
+        ob = T.Beam(coords, 1., beam.charge, beam.mass, beam.circumference,
+                    beam.gamma)
+        T.LinearMap([alpha], beam.circumference, Qs).track(ob)
+        np.testing.assert_array_equal(beam.dp.cpu().numpy(), ob.dp,
+                                      err_msg='divisor set %d' % i)
+        np.testing.assert_array_equal(beam.z.cpu().numpy(), ob.z)
