@@ -9,8 +9,8 @@
  *   0      success
  *   < 0    argument error detected on the host before any launch
  *          (PHK_E* below); the message is available from phk_last_error()
- *   > 0    never returned by a call; device-side error words are written to
- *          the caller's status buffer where an entry point takes one.
+ *   > 0    never returned by a call; device-side errors (PHK_DEV_*) are
+ *          written to the optional status word of phk_program.
  *
  * Citations are path:line in the PyHEADTAIL source tree.
  *
@@ -159,11 +159,17 @@ typedef struct phk_detuner {
     double c[16];
 } phk_detuner;
 
+/* status (optional, device int32): a kernel that gives up a bounded wait
+ * (a bulk copy that never completed) stores PHK_DEV_TIMEOUT there, stops
+ * processing, drains its copies in flight and returns; the caller reads
+ * it after synchronising.  NULL: no report. */
+#define PHK_DEV_TIMEOUT 1
 typedef struct phk_program {
     int32_t n_ops;
     int32_t n_det;
     phk_op op[PHK_MAX_OPS];
     phk_detuner det[PHK_MAX_DETUNERS];
+    int32_t *status;
 } phk_program;
 
 /* ---- wake kicks applied to particles: DipoleWakeKickX/Y.apply

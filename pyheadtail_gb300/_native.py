@@ -11,6 +11,7 @@ import os
 from . import _build
 
 PHK_F64, PHK_F32 = 0, 1
+PHK_DEV_TIMEOUT = 1
 PHK_MAX_OPS = 12
 PHK_MAX_DETUNERS = 6
 PHK_MAX_POLY = 8
@@ -60,7 +61,8 @@ class Detuner(ctypes.Structure):
 
 class Program(ctypes.Structure):
     _fields_ = [('n_ops', ctypes.c_int32), ('n_det', ctypes.c_int32),
-                ('op', Op * PHK_MAX_OPS), ('det', Detuner * PHK_MAX_DETUNERS)]
+                ('op', Op * PHK_MAX_OPS), ('det', Detuner * PHK_MAX_DETUNERS),
+                ('status', ctypes.c_void_p)]
 
 
 class KickSet(ctypes.Structure):

@@ -558,7 +558,7 @@ struct TrackArgs {
     int32_t n_hist;      // histogram copies per CTA (1 or warps per CTA)
     int32_t kicks_smem;  // kick tables staged in shared memory
     int32_t cluster;     // CTAs per thread-block cluster (accumulation)
-    int32_t reserved;
+    int32_t stages;      // TMA ring stages (0: plain loads)
 };
 
 template <typename T>
@@ -578,12 +578,14 @@ __device__ __forceinline__ float tmul<float>(float a, float b) { return a * b; }
 //   histogram words  [3][n_hist][Sa]   (sum x, sum y as Hist<T>::Word; count
 //                                       as int in the third region)
 //   accumulation edges [Sa + 1] T, pending-kick edges [Sp + 1] T,
-//   kick tables [n_kicks][Sp] T (when staged), bid tags [n_hist][Sa] int
+//   kick tables [n_kicks][Sp] T (when staged), bid tags [n_hist][Sa] int,
+//   TMA ring [stages][6][tile] T, one mbarrier per stage
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
 template <typename T>
 __host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
                                                     int n_kicks, int kicks_smem,
+                                                    int stages, int tile,
                                                     size_t* off) {
     size_t b = 0;
     off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x words
@@ -593,6 +595,8 @@ __host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
     off[4] = b; b = align16(b + sizeof(T) * (Sp > 0 ? Sp + 1 : 0));
     off[5] = b; b = align16(b + (kicks_smem ? sizeof(T) * (size_t)n_kicks * Sp : 0));
     off[6] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // bid tags
+    off[7] = b; b = align16(b + (size_t)stages * 6 * tile * sizeof(T));
+    off[8] = b; b = align16(b + (size_t)8 * stages);         // mbarriers
     return b;
 }
 
@@ -647,18 +651,127 @@ struct Bins<double> {
     }
 };
 
+// Per-CTA state shared by the tile loops of the track kernel.
 template <typename T, int VEC>
-__global__ void __launch_bounds__(kTrackThreads)
+struct TrackCtx {
+    using W = typename Hist<T>::Word;
+    T* cp[6];
+    Bins<T> bpk, bac;
+    const T* ktab;
+    W* hx;
+    W* hy;
+    int* hc;
+    int* tag;
+    unsigned epoch;
+    bool shared_hist;
+};
+
+// One tile of VEC particles per thread, already in registers: pending
+// kicks, element program, slice accumulation; then the stores.  All threads
+// of the CTA call this together (the accumulation is warp-synchronous);
+// lanes whose particles are past the end pass live = false.
+template <typename T, int VEC>
+__device__ __forceinline__ void run_tile(const phk_program& prog,
+                                         const phk_kick_set& pk,
+                                         const phk_accum& acc,
+                                         const TrackArgs& a,
+                                         TrackCtx<T, VEC>& cx, Tile<T, VEC>& t,
+                                         int64_t i0, bool full) {
+    const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
+    const int nk = a.has_pk ? pk.n_kicks : 0;
+    // 1. wake kicks of the previous WakeField.track, in kick order
+    if (a.has_pk) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const int s = cx.bpk.index(t.c[PHK_Z][j]);
+            if (s < 0 || i0 + j >= a.n) continue;
+            const T kx = t.c[PHK_X][j], ky = t.c[PHK_Y][j];
+            for (int k = 0; k < nk; ++k) {
+                T val = a.kicks_smem
+                            ? cx.ktab[k * Sp + s]
+                            : __ldg(reinterpret_cast<const T*>(pk.kick[k]) + s);
+                const int qd = pk.quad[k];
+                if (qd == PHK_X) val = tmul<T>(val, kx);
+                else if (qd == PHK_Y) val = tmul<T>(val, ky);
+                const int tg = pk.target[k];
+                if (tg == PHK_XP) t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], val);
+                else if (tg == PHK_YP) t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], val);
+                else t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], val);
+            }
+        }
+    }
+    // 2. element program
+    run_program<T, VEC>(prog, t);
+    // 3. slice accumulation
+    if (a.has_acc) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const bool live = i0 + j < a.n;
+            const int s = live ? cx.bac.index(t.c[PHK_Z][j]) : -1;
+            if (acc.idx_out && live)
+                acc.idx_out[i0 + j] =
+                    s >= 0 ? s
+                           : outside_index((double)t.c[PHK_Z][j],
+                                           acc.slicer.tail, acc.slicer.width);
+            warp_accumulate<T>(s, t.c[PHK_X][j], t.c[PHK_Y][j], cx.hx, cx.hy,
+                               cx.hc, cx.tag, cx.epoch, cx.shared_hist);
+        }
+    }
+    // 4. stores of the coordinates the tile changed
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        if (!((a.store_mask >> q) & 1)) continue;
+        if (full) {
+            VecIO<T, VEC>::st(cx.cp[q] + i0, t.c[q]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j)
+                if (i0 + j < a.n) cx.cp[q][i0 + j] = t.c[q][j];
+        }
+    }
+}
+
+template <typename T, int VEC>
+__device__ __forceinline__ void load_tile_plain(const TrackArgs& a,
+                                                const TrackCtx<T, VEC>& cx,
+                                                Tile<T, VEC>& t, int64_t i0,
+                                                bool full) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        if (!((a.load_mask >> q) & 1)) {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
+            continue;
+        }
+        if (full) {
+            VecIO<T, VEC>::ld(cx.cp[q] + i0, t.c[q]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j)
+                t.c[q][j] = (i0 + j < a.n) ? cx.cp[q][i0 + j] : T(0);
+        }
+    }
+}
+
+// polls of one mbarrier phase before a kernel gives up (order of a second)
+constexpr unsigned kWaitLimit = 1u << 22;
+
+// FP32 launches aim at two resident CTAs per SM (<= 128 registers), FP64
+// ones at one (FP64-pipe bound; registers hold the long FP64 chains)
+template <typename T, int VEC>
+__global__ void __launch_bounds__(kTrackThreads, sizeof(T) == 4 ? 2 : 1)
 track_kernel(const __grid_constant__ phk_program prog,
              const __grid_constant__ phk_kick_set pk,
              const __grid_constant__ phk_accum acc, const TrackArgs a) {
     using W = typename Hist<T>::Word;
     extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int TILE = kTrackThreads * VEC;
     const int Sa = a.has_acc ? acc.slicer.n_slices : 0;
     const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
     const int nk = a.has_pk ? pk.n_kicks : 0;
-    size_t off[7];
-    track_smem_layout<T>(Sa, Sp, a.n_hist, nk, a.kicks_smem, off);
+    size_t off[9];
+    track_smem_layout<T>(Sa, Sp, a.n_hist, nk, a.kicks_smem, a.stages, TILE,
+                         off);
     W* hsx = reinterpret_cast<W*>(smem + off[0]);
     W* hsy = reinterpret_cast<W*>(smem + off[1]);
     int* hcnt = reinterpret_cast<int*>(smem + off[2]);
@@ -666,8 +779,16 @@ track_kernel(const __grid_constant__ phk_program prog,
     T* epk = reinterpret_cast<T*>(smem + off[4]);
     T* ktab = reinterpret_cast<T*>(smem + off[5]);
     int* htag = reinterpret_cast<int*>(smem + off[6]);
+    T* ring = reinterpret_cast<T*>(smem + off[7]);
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + off[8]);
+    __shared__ int s_fail;
 
     const int tid = threadIdx.x;
+    if (tid == 0) {
+        s_fail = 0;
+        for (int st = 0; st < a.stages; ++st) mbar_init(bars + st, 1);
+        if (a.stages > 0) mbar_fence_init();
+    }
     if (a.has_acc) {
         const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
         for (int i = tid; i <= Sa; i += blockDim.x) stage_edge<T>(eacc, i, e[i]);
@@ -687,94 +808,96 @@ track_kernel(const __grid_constant__ phk_program prog,
     }
     __syncthreads();
 
-    // first-estimate parameters of the two bin searches, from the tables
-    Bins<T> bpk, bac;
-    if (a.has_pk) bpk.init(epk, Sp, pk.slicer.negate);
-    if (a.has_acc) bac.init(eacc, Sa, acc.slicer.negate);
+    TrackCtx<T, VEC> cx;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) cx.cp[q] = reinterpret_cast<T*>(a.c[q]);
+    if (a.has_pk) cx.bpk.init(epk, Sp, pk.slicer.negate);
+    if (a.has_acc) cx.bac.init(eacc, Sa, acc.slicer.negate);
+    cx.ktab = ktab;
     const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
-    const bool shared_hist = a.n_hist < (int)(blockDim.x >> 5);
-    W* my_sx = hsx + h * Sa;
-    W* my_sy = hsy + h * Sa;
-    int* my_cnt = hcnt + h * Sa;
-    int* my_tag = htag + h * Sa;
-    unsigned epoch = 0;
+    cx.hx = hsx + h * Sa;
+    cx.hy = hsy + h * Sa;
+    cx.hc = hcnt + h * Sa;
+    cx.tag = htag + h * Sa;
+    cx.epoch = 0;
+    cx.shared_hist = a.n_hist < (int)(blockDim.x >> 5);
 
-    T* cp[6];
+    if (a.stages > 0) {
+        // ---- full tiles through a TMA ring: thread 0 keeps `stages` tiles
+        // of bulk copies in flight while the CTA computes
+        const int64_t full_tiles = a.n / TILE;
+        const int64_t mine = blockIdx.x < full_tiles
+                                 ? (full_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x
+                                 : 0;
+        int nq = 0;
+        for (int q = 0; q < 6; ++q) nq += (a.load_mask >> q) & 1;
+        const unsigned stage_bytes = (unsigned)(nq * TILE * sizeof(T));
+        auto issue = [&](int64_t k) {
+            const int st = (int)(k % a.stages);
+            const int64_t tile = blockIdx.x + k * gridDim.x;
+            fence_proxy_async_smem();
+            mbar_expect_tx(bars + st, stage_bytes);
+            for (int q = 0; q < 6; ++q)
+                if ((a.load_mask >> q) & 1)
+                    bulk_g2s(ring + ((size_t)st * 6 + q) * TILE,
+                             cx.cp[q] + tile * TILE, TILE * sizeof(T),
+                             bars + st);
+        };
+        int64_t issued = 0;
+        if (tid == 0)
+            for (; issued < mine && issued < a.stages; ++issued) issue(issued);
+        int64_t k = 0;
+        for (; k < mine; ++k) {
+            const int st = (int)(k % a.stages);
+            const unsigned parity = (unsigned)((k / a.stages) & 1);
+            if (!mbar_wait(bars + st, parity, kWaitLimit)) s_fail = 1;
+            __syncthreads();
+            if (s_fail) break;
+            Tile<T, VEC> t;
+            const T* src = ring + (size_t)st * 6 * TILE + tid * VEC;
 #pragma unroll
-    for (int q = 0; q < 6; ++q) cp[q] = reinterpret_cast<T*>(a.c[q]);
-
-    // every warp runs whole tiles (lanes past the end carry dead particles)
-    // so that the warp-level slice accumulation sees all 32 lanes
-    const int64_t n_tiles_grid = (a.n_tiles + gridDim.x - 1) / gridDim.x;
-    for (int64_t it = 0; it < n_tiles_grid; ++it) {
-        const int64_t tile = blockIdx.x + it * gridDim.x;
-        const int64_t i0 = (tile * blockDim.x + tid) * VEC;
-        const bool full = i0 + VEC <= a.n;
-        Tile<T, VEC> t;
+            for (int q = 0; q < 6; ++q) {
+                if ((a.load_mask >> q) & 1) {
+                    VecIO<T, VEC>::ld(src + (size_t)q * TILE, t.c[q]);
+                } else {
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            if (!((a.load_mask >> q) & 1)) {
-#pragma unroll
-                for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
-                continue;
-            }
-            if (full) {
-                VecIO<T, VEC>::ld(cp[q] + i0, t.c[q]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < VEC; ++j)
-                    t.c[q][j] = (i0 + j < a.n) ? cp[q][i0 + j] : T(0);
-            }
-        }
-        // 1. wake kicks of the previous WakeField.track, in kick order
-        if (a.has_pk) {
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-                const int s = bpk.index(t.c[PHK_Z][j]);
-                if (s < 0 || i0 + j >= a.n) continue;
-                const T kx = t.c[PHK_X][j], ky = t.c[PHK_Y][j];
-                for (int k = 0; k < nk; ++k) {
-                    T val = a.kicks_smem
-                                ? ktab[k * Sp + s]
-                                : __ldg(reinterpret_cast<const T*>(pk.kick[k]) + s);
-                    const int qd = pk.quad[k];
-                    if (qd == PHK_X) val = tmul<T>(val, kx);
-                    else if (qd == PHK_Y) val = tmul<T>(val, ky);
-                    const int tg = pk.target[k];
-                    if (tg == PHK_XP) t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], val);
-                    else if (tg == PHK_YP) t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], val);
-                    else t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], val);
+                    for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
                 }
             }
+            const int64_t i0 = (blockIdx.x + k * gridDim.x) * TILE + tid * VEC;
+            run_tile<T, VEC>(prog, pk, acc, a, cx, t, i0, true);
+            __syncthreads();                 // stage st fully read
+            if (tid == 0 && k + a.stages < mine) issue(k + a.stages), ++issued;
         }
-        // 2. element program
-        run_program<T, VEC>(prog, t);
-        // 3. slice accumulation
-        if (a.has_acc) {
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-                const bool live = i0 + j < a.n;
-                const int s = live ? bac.index(t.c[PHK_Z][j]) : -1;
-                if (acc.idx_out && live)
-                    acc.idx_out[i0 + j] =
-                        s >= 0 ? s
-                               : outside_index((double)t.c[PHK_Z][j],
-                                               acc.slicer.tail,
-                                               acc.slicer.width);
-                warp_accumulate<T>(s, t.c[PHK_X][j], t.c[PHK_Y][j], my_sx,
-                                   my_sy, my_cnt, my_tag, epoch, shared_hist);
+        if (s_fail) {
+            // report, then wait (bounded) for this CTA's copies in flight so
+            // that none lands in shared memory after the CTA has exited
+            if (tid == 0) {
+                if (prog.status) atomicMax(prog.status, PHK_DEV_TIMEOUT);
+                for (int64_t j = k; j < issued; ++j)
+                    mbar_wait(bars + (int)(j % a.stages),
+                              (unsigned)((j / a.stages) & 1), kWaitLimit);
             }
+            __syncthreads();
+        } else if (a.n % TILE != 0 && blockIdx.x == (int)(full_tiles % gridDim.x)) {
+            // ---- the partial last tile, plain loads
+            const int64_t i0 = full_tiles * TILE + tid * VEC;
+            const bool full = i0 + VEC <= a.n;
+            Tile<T, VEC> t;
+            load_tile_plain<T, VEC>(a, cx, t, i0, full);
+            run_tile<T, VEC>(prog, pk, acc, a, cx, t, i0, full);
         }
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            if (!((a.store_mask >> q) & 1)) continue;
-            if (full) {
-                VecIO<T, VEC>::st(cp[q] + i0, t.c[q]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < VEC; ++j)
-                    if (i0 + j < a.n) cp[q][i0 + j] = t.c[q][j];
-            }
+    } else {
+        // ---- plain loads; every warp runs whole tiles (lanes past the end
+        // carry dead particles) so the warp-level accumulation sees 32 lanes
+        const int64_t n_tiles_grid = (a.n_tiles + gridDim.x - 1) / gridDim.x;
+        for (int64_t it = 0; it < n_tiles_grid; ++it) {
+            const int64_t tile = blockIdx.x + it * gridDim.x;
+            const int64_t i0 = (tile * blockDim.x + tid) * VEC;
+            const bool full = i0 + VEC <= a.n;
+            Tile<T, VEC> t;
+            load_tile_plain<T, VEC>(a, cx, t, i0, full);
+            run_tile<T, VEC>(prog, pk, acc, a, cx, t, i0, full);
         }
     }
 
@@ -835,26 +958,41 @@ struct TrackCfg {
     static constexpr int VEC = sizeof(T) == 8 ? 2 : 4;
 };
 
-// histogram copies: one per warp while they fit in 96 KB, else one per CTA
+// Shared-memory plan of a launch: histogram copies (one private copy per
+// warp when they fit, else fewer copies shared with atomics) and TMA ring
+// stages (FP32 aligned launches), chosen so that two CTAs fit on an SM
+// whenever possible.
 template <typename T>
-static int hist_copies(int Sa) {
-    if (Sa <= 0) return 1;
+static size_t smem_for(int Sa, int Sp, int nk, bool tma, int* n_hist,
+                       int* kicks_smem, int* stages) {
     const int warps = kTrackThreads / 32;
-    return (size_t)warps * Sa * 24 <= 112 * 1024 ? warps : 1;
-}
-
-template <typename T>
-static size_t smem_for(int Sa, int Sp, int nk, int* n_hist, int* kicks_smem) {
-    size_t off[7];
-    *n_hist = hist_copies<T>(Sa);
+    const int tile = kTrackThreads * (sizeof(T) == 8 ? 2 : 4);
     *kicks_smem = (size_t)nk * Sp * sizeof(T) <= 48 * 1024;
-    return track_smem_layout<T>(Sa, Sp, *n_hist, nk, *kicks_smem, off);
+    const int hist_opts[4] = {warps, 4, 2, 1};
+    const int stage_opts[2] = {3, 2};
+    size_t off[9];
+    size_t best = 0;
+    for (int hi = 0; hi < 4; ++hi) {
+        for (int si = 0; si < (tma ? 2 : 1); ++si) {
+            const int nh = Sa > 0 ? hist_opts[hi] : 1;
+            const int st = tma ? stage_opts[si] : 0;
+            const size_t b = track_smem_layout<T>(Sa, Sp, nh, nk, *kicks_smem,
+                                                  st, tile, off);
+            if (best == 0 || b <= 112 * 1024) {
+                *n_hist = nh;
+                *stages = st;
+                best = b;
+            }
+            if (b <= 112 * 1024) return b;
+        }
+    }
+    return best;
 }
 
 size_t track_smem_bytes(int32_t dtype, int32_t Sa, int32_t Sp) {
-    int nh, ks;
-    return dtype == PHK_F64 ? smem_for<double>(Sa, Sp, 4, &nh, &ks)
-                            : smem_for<float>(Sa, Sp, 4, &nh, &ks);
+    int nh, ks, st;
+    return dtype == PHK_F64 ? smem_for<double>(Sa, Sp, 4, false, &nh, &ks, &st)
+                            : smem_for<float>(Sa, Sp, 4, true, &nh, &ks, &st);
 }
 
 // Opt the track kernel into the device's full dynamic shared memory, once
@@ -938,7 +1076,7 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     a.load_mask = load_mask;
     a.store_mask = store_mask;
     a.cluster = 1;
-    a.reserved = 0;
+    a.stages = 0;
     const int64_t per_tile = (int64_t)kTrackThreads * VEC;
     a.n_tiles = (c->n + per_tile - 1) / per_tile;
     static phk_kick_set zero_pk;
@@ -946,7 +1084,11 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     const int Sa = acc ? acc->slicer.n_slices : 0;
     const int Sp = pk ? pk->slicer.n_slices : 0;
     const int nk = pk ? pk->n_kicks : 0;
-    const size_t smem = smem_for<T>(Sa, Sp, nk, &a.n_hist, &a.kicks_smem);
+    // the TMA ring needs 16-byte aligned coordinates (VEC > 1 launches)
+    // and pays off for the memory-bound FP32 form
+    const bool tma = VEC > 1 && sizeof(T) == 4;
+    const size_t smem = smem_for<T>(Sa, Sp, nk, tma, &a.n_hist,
+                                    &a.kicks_smem, &a.stages);
     if (smem > (size_t)device_info().max_smem_optin)
         return set_error(PHK_ESIZE, "phk_track: %zu bytes of shared memory "
                          "needed for %d + %d slices", smem, Sa, Sp);

@@ -91,7 +91,7 @@ def test_struct_layout_matches_header():
     assert ctypes.sizeof(N.Slicer) == 48
     assert ctypes.sizeof(N.Op) == 24 + 32 * 8
     assert ctypes.sizeof(N.Detuner) == 24 + 16 * 8
-    assert ctypes.sizeof(N.Program) == 8 + 12 * 280 + 6 * 152
+    assert ctypes.sizeof(N.Program) == 8 + 12 * 280 + 6 * 152 + 8
     assert N.KickSet.kick.offset == 120
     assert ctypes.sizeof(N.KickSet) == 184
     assert ctypes.sizeof(N.Accum) == 80
