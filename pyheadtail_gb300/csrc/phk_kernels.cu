@@ -1003,10 +1003,29 @@ static void prepare_track_kernel() {
     const DeviceInfo& d = device_info();
     const int dev = d.device < 64 ? d.device : 63;
     if (done_for[dev]) return;
-    cudaFuncSetAttribute(track_kernel<T, VEC>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         d.max_smem_optin);
+    // dynamic + static shared memory must stay within the opt-in limit
+    cudaFuncAttributes fa;
+    size_t static_smem = 0;
+    if (cudaFuncGetAttributes(&fa, track_kernel<T, VEC>) == cudaSuccess)
+        static_smem = fa.sharedSizeBytes;
+    else
+        cudaGetLastError();
+    if (cudaFuncSetAttribute(track_kernel<T, VEC>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             d.max_smem_optin - (int)static_smem) != cudaSuccess)
+        cudaGetLastError();
     done_for[dev] = 1;
+}
+
+// largest dynamic shared memory a track launch may request
+template <typename T, int VEC>
+static size_t track_dynamic_smem_limit() {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, track_kernel<T, VEC>) != cudaSuccess) {
+        cudaGetLastError();
+        return (size_t)device_info().max_smem_optin - 1024;
+    }
+    return (size_t)device_info().max_smem_optin - fa.sharedSizeBytes;
 }
 
 // CTAs per thread-block cluster of an accumulating launch
@@ -1089,7 +1108,7 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     const bool tma = VEC > 1 && sizeof(T) == 4;
     const size_t smem = smem_for<T>(Sa, Sp, nk, tma, &a.n_hist,
                                     &a.kicks_smem, &a.stages);
-    if (smem > (size_t)device_info().max_smem_optin)
+    if (smem > track_dynamic_smem_limit<T, VEC>())
         return set_error(PHK_ESIZE, "phk_track: %zu bytes of shared memory "
                          "needed for %d + %d slices", smem, Sa, Sp);
     prepare_track_kernel<T, VEC>();
