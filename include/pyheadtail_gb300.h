@@ -295,6 +295,29 @@ int phk_slice_moments(const phk_slicer *slicer, const void *z, int64_t n,
                       int32_t pass, const double *means, double *sums,
                       int32_t *counts, void *stream);
 
+/* Slicing pass that allocates nothing and takes no workspace; no
+ * counterpart in the reference.  Same results as phk_track(empty program,
+ * coords, NULL, acc) followed by phk_slice_finalize(acc, counts, mean_x,
+ * mean_y, NULL): per-slice counts and centroids of x, y binned on z
+ * (slicing.py:96-113, 253-262).  For callers that cannot allocate device
+ * memory (a host runtime that holds only device pointers given to it, or
+ * whose device memory belongs to another allocator's fixed pool).
+ *   - The partial sums live in a library-owned device array of
+ *     3 * 512 * 128 doubles (1.5 MiB, loaded with the library): n_slices
+ *     must be <= 512, else PHK_ESIZE and nothing runs.
+ *   - Its device address is looked up (cudaGetSymbolAddress) on the first
+ *     call on each device, with that device current; make that first call
+ *     before any stream capture.
+ *   - Nothing needs zeroing: every call rewrites the part it reads.
+ *   - All calls on a device share the array: calls whose kernels can
+ *     overlap (different streams without ordering between them) race.
+ *   - coords->xp, yp, dp are not read and may be NULL.
+ * counts, mean_x, mean_y: device arrays of n_slices entries (any may be
+ * NULL).  Allocates no device or host memory. */
+int phk_slice_noalloc(const phk_slicer *slicer, const phk_coords *coords,
+                      int32_t *counts, double *mean_x, double *mean_y,
+                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif

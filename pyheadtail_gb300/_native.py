@@ -117,6 +117,9 @@ SIGNATURES = {
                           ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
                           ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p, ctypes.c_void_p],
+    'phk_slice_noalloc': [ctypes.POINTER(Slicer), ctypes.POINTER(Coords),
+                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_void_p],
 }
 
 _lib = None
