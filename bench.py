@@ -56,6 +56,14 @@ WORKLOADS = {
                      'resonator + 50-turn resistive wall'),
 }
 
+# the batched workload: 256 bunches, sizes / chromaticities / intensities
+# drawn with seed 3, 100 slices each, resonator wake, RF as C2
+C4 = dict(n_bunches=256, seed=3, slices=100, chroma=(-5., 15.),
+          intensity=(5e10, 2e11), log10_n=(4., 6.),
+          label="C4: 256 bunches in one persistent launch, N_b log-uniform "
+                "in [1e4, 1e6], own Q' in [-5, 15] and intensity in "
+                "[5e10, 2e11], 100 slices each, resonator, RF h=4620")
+
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -431,6 +439,289 @@ def run_ours(a, rank, world):
     print(json.dumps(out))
 
 
+# ------------------------------------------------------------ batched arm
+
+def c4_draws():
+    rs = np.random.RandomState(C4['seed'])
+    nb = C4['n_bunches']
+    sizes = np.round(10 ** rs.uniform(*C4['log10_n'], size=nb)).astype(
+        np.int64)
+    chroma = rs.uniform(*C4['chroma'], size=nb)
+    intensity = rs.uniform(*C4['intensity'], size=nb)
+    return sizes, chroma, intensity
+
+
+def c4_coords(n, b, precision, device='cuda'):
+    """Matched Gaussian bunch of n particles drawn on the device with a
+    per-bunch seed (same sigmas as the single-bunch workloads)."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(3000 + b)
+    eps = 2.5e-6 / np.sqrt(GAMMA**2 - 1)
+    sig = {'x': np.sqrt(eps * 50.), 'xp': np.sqrt(eps / 50.),
+           'y': np.sqrt(eps * 50.), 'yp': np.sqrt(eps / 50.),
+           'z': 0.23, 'dp': 1e-3}
+    dt = torch.float64 if precision == 'fp64' else torch.float32
+    return {k: (torch.randn(n, generator=g, device=device,
+                            dtype=torch.float64) * s).to(dt)
+            for k, s in sig.items()}
+
+
+def c4_bunch(n, q, intensity, coords, precision):
+    from scipy.constants import e, m_p
+    from pyheadtail_gb300.general.printers import SilentPrinter
+    from pyheadtail_gb300.impedances import wakes as W
+    from pyheadtail_gb300.particles.particles import Particles
+    from pyheadtail_gb300.particles.slicing import UniformBinSlicer
+    from pyheadtail_gb300.trackers.detuners import Chromaticity
+    from pyheadtail_gb300.trackers.longitudinal_tracking import RFSystems
+    from pyheadtail_gb300.trackers.transverse_tracking import TransverseMap
+    sp = SilentPrinter()
+    beam = Particles(n, intensity / n, e, m_p, C_RING, GAMMA,
+                     coords_n_momenta_dict=coords, precision=precision)
+    z2 = np.zeros(2)
+    tm = TransverseMap(np.array([0., C_RING]), z2, np.array([50., 50.]), z2,
+                       z2, np.array([50., 50.]), z2, 20.13, 20.18,
+                       [Chromaticity(q, q)], printer=sp)
+    rf = RFSystems(C_RING, [4620], [4.5e6], [0.], [ALPHA_C], GAMMA,
+                   charge=e, mass=m_p, printer=sp, warningprinter=sp)
+    wf = W.WakeField(UniformBinSlicer(C4['slices'], z_cuts=Z_CUTS,
+                                      warningprinter=sp),
+                     W.CircularResonator(10e6, 1e9, 1.))
+    return beam, list(tm) + [rf, wf]
+
+
+def time_batch(precision, steps, warmup, flush, autotune):
+    import torch
+    from pyheadtail_gb300 import _native as N
+    from pyheadtail_gb300.batch import BatchedTurn, BunchBatch
+    sizes, chroma, intensity = c4_draws()
+    beams, maps = [], []
+    for b in range(len(sizes)):
+        c = c4_coords(int(sizes[b]), b, precision)
+        beam, els = c4_bunch(int(sizes[b]), float(chroma[b]),
+                             float(intensity[b]), c, precision)
+        beams.append(beam)
+        maps.append(els)
+    batch = BunchBatch(beams)
+    turn = BatchedTurn(batch, maps, autotune=autotune)
+    turn.track(max(warmup, 3))           # eager warm-up, then capture
+    for _ in range(20):
+        if turn._graph is not None:
+            break
+        turn.track(1)
+    if turn._graph is None:
+        raise RuntimeError('batched turn did not become stationary')
+    turn.track(1)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for i in range(steps):
+        flush_l2(flush)
+        torch.cuda._sleep(SPIN_CYCLES)
+        starts[i].record()
+        turn.replay_turns(1)
+        ends[i].record()
+    torch.cuda.synchronize()
+    graph_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    # library kernels in one captured turn
+    kernels_per_turn = turn.kernels_per_turn
+    del N
+    # the batched track kernel alone: eager turns with events around it
+
+    def spaced():
+        flush_l2(flush)
+        torch.cuda._sleep(SPIN_CYCLES)
+    turn.track_events = []
+    turn.before_track = spaced
+    turn.eager_turns(steps)
+    turn.before_track = None
+    torch.cuda.synchronize()
+    track_ms = [a.elapsed_time(b) for a, b in turn.track_events]
+    turn.track_events = None
+    # e2e: every bunch's coordinates from pinned host memory into the
+    # batch, one turn, the per-bunch centroids read back
+    host = {k: torch.empty(batch.total, dtype=batch.storage[k].dtype
+                           ).pin_memory() for k in batch.storage}
+    for k in host:
+        host[k].copy_(batch.storage[k][:batch.total])
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    e2e_s = []
+    for i in range(max(3, steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k, t in host.items():
+            batch.storage[k][:batch.total].copy_(t, non_blocking=True)
+        turn.track(1)
+        cx, cy = turn.bunch_centroids()
+        res = torch.stack([cx, cy]).cpu()
+        e2e_s.append(time.perf_counter() - t0)
+    return dict(graph_ms=graph_ms, track_ms=track_ms, e2e_s=e2e_s, h2d=h2d,
+                d2h=res.numel() * 8, kernels_per_turn=kernels_per_turn,
+                total=int(batch.total), particles=int(sizes.sum()),
+                config=dict(turn.config), grid=turn._p['grid'],
+                units=len(turn._p['plan']['units']),
+                columns=turn._p['plan']['n_columns'])
+
+
+def c4_oracle_sample(budget_s=12.0):
+    """Oracle on a bounded sample of the batch: its first bunches up to
+    ~3e5 particles, turns until about budget_s of single-thread time."""
+    from scipy.constants import e, m_p
+    from oracle import turn_loop as T
+    sizes, chroma, intensity = c4_draws()
+    runs, tot = [], 0
+    for b in range(len(sizes)):
+        n = int(sizes[b])
+        if tot and tot + n > 300000:
+            continue
+        rng = np.random.RandomState(3000 + b)
+        eps = 2.5e-6 / np.sqrt(GAMMA**2 - 1)
+        sig = {'x': np.sqrt(eps * 50.), 'xp': np.sqrt(eps / 50.),
+               'y': np.sqrt(eps * 50.), 'yp': np.sqrt(eps / 50.),
+               'z': 0.23, 'dp': 1e-3}
+        coords = {k: rng.normal(0, s, n) for k, s in sig.items()}
+        beam = T.Beam(coords, intensity[b] / n, e, m_p, C_RING, GAMMA)
+        z2 = np.zeros(2)
+        segs = T.transverse_map([0., C_RING], z2, np.array([50., 50.]), z2,
+                                z2, np.array([50., 50.]), z2, 20.13, 20.18,
+                                chroma=(chroma[b], chroma[b]), amplitude=None)
+        lm = T.RFSystems(C_RING, [4620], [4.5e6], [0.], [ALPHA_C], GAMMA,
+                         charge=e, mass=m_p)
+        sl = T.UniformBinSlicer(C4['slices'], z_cuts=Z_CUTS)
+        wf = T.WakeField(sl, T.circular_resonator_kicks(sl, 10e6, 1e9, 1.), 1)
+        runs.append((beam, list(segs) + [lm, wf]))
+        tot += n
+        if tot >= 300000:
+            break
+    for beam, els in runs:
+        for m in els:
+            m.track(beam)
+    t0 = time.perf_counter()
+    turns = 0
+    while True:
+        for beam, els in runs:
+            for m in els:
+                m.track(beam)
+        turns += 1
+        if time.perf_counter() - t0 > budget_s or turns >= 200:
+            break
+    dt = time.perf_counter() - t0
+    return tot * turns / dt, tot, turns, len(runs)
+
+
+def run_batch(a, rank, world):
+    import torch
+    dev = rank % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32,
+                        device='cuda')
+    hbm_peak, peak_kind = measured_peaks()
+    steps = a.steps if a.steps_given else 50
+    sampler = ClockSampler(dev)
+    forms = {}
+    sampler.start()
+    for precision in ('fp32', 'fp64'):
+        if a.form not in ('all', precision):
+            continue
+        r = time_batch(precision, steps, a.warmup, flush, a.autotune)
+        bytes_pp = 96 if precision == 'fp64' else 48
+        n = r['particles']
+        step_ms = float(np.sum(r['graph_ms']))
+        track_avg = float(np.mean(r['track_ms']))
+        achieved = bytes_pp * n / (track_avg * 1e-3) / 1e9
+        tpp = profile_traffic('track_batch_c4_%s' % precision)
+        e2e_t = float(np.sum(r['e2e_s']))
+        forms[precision] = {
+            'value': n * steps / (step_ms * 1e-3),
+            'ms_per_step': step_ms / steps,
+            'kernels_per_turn': r['kernels_per_turn'],
+            'launch': {'config': r['config'], 'grid': r['grid'],
+                       'units': r['units'], 'columns': r['columns']},
+            'roofline': {'bound': 'hbm', 'achieved': achieved,
+                         'peak': hbm_peak, 'unit': 'GB/s',
+                         'frac': achieved / hbm_peak, 'peak_kind': peak_kind,
+                         'traffic': None if tpp is None else tpp * n,
+                         'kernel': 'phk::batch_track_kernel',
+                         'kernel_ms': track_avg,
+                         'algorithmic_bytes_per_launch': bytes_pp * n},
+            'e2e': {'value': n * len(r['e2e_s']) / e2e_t,
+                    'unit': 'macroparticle-turns/s',
+                    'h2d_bytes_per_step': r['h2d'],
+                    'd2h_bytes_per_step': r['d2h']},
+            'particles': n,
+        }
+    clocks = sampler.stop()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([max(f['ms_per_step'] for f in forms.values())],
+                         device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    if rank != 0:
+        return
+    prec = 'fp32' if 'fp32' in forms else 'fp64'
+    head = forms[prec]
+    out = {
+        'metric': 'macroparticle-turns/s on 1 GB300: FP32/batched vs FP64 '
+                  'plain; % HBM roofline',
+        'value': head['value'] * world,
+        'unit': 'macroparticle-turns/s',
+        'n_gpus': world, 'steps': steps, 'warmup': a.warmup,
+        'ms_per_step': head['ms_per_step'],
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32' if prec == 'fp32' else 'f64',
+        'data': 'synthetic: 256 seeded matched Gaussian bunches drawn on the '
+                'device, no dataset',
+        'config': {'workload': C4['label'],
+                   'n_macroparticles': head['particles'],
+                   'n_bunches': C4['n_bunches'], 'n_slices': C4['slices'],
+                   'form': 'batched ' + prec, 'turns_per_step': 1,
+                   'l2': 'flushed between steps (512 MiB write + 256 MiB '
+                         'read-back, untimed); working set larger than L2',
+                   'timing': 'CUDA events around a CUDA-graph replay of the '
+                             'batched turn; inputs resident in HBM',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'roofline': head['roofline'],
+        'e2e': head['e2e'],
+        'gpu_launches': head['kernels_per_turn'] * steps,
+        'clocks': clocks,
+        'forms': forms,
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        v, tot, turns, nbs = c4_oracle_sample()
+        out['cpu_baseline'] = {
+            'value': v, 'unit': 'macroparticle-turns/s', 'cores': 1,
+            'kind': 'port',
+            'sample': '%d macroparticles (%d bunches of the batch) x %d '
+                      'turns (oracle, single thread)' % (tot, nbs, turns)}
+    print(json.dumps(out))
+
+
+def run_reference_c4(a, rank, world):
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    v, tot, turns, nbs = c4_oracle_sample(budget_s=max(2.0, 0.2 * a.steps))
+    del t0
+    sample = ('%d macroparticles (%d bunches of the batch) x %d turns'
+              % (tot, nbs, turns))
+    print(json.dumps({
+        'impl': 'reference',
+        'metric': 'macroparticle-turns/s on 1 GB300: FP32/batched vs FP64 '
+                  'plain; % HBM roofline',
+        'value': v, 'unit': 'macroparticle-turns/s', 'n_gpus': world,
+        'steps': a.steps, 'warmup': a.warmup,
+        'ms_per_step': tot / v * 1e3, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic: seeded matched Gaussian bunches',
+        'config': {'workload': C4['label'], 'n_bunches': C4['n_bunches'],
+                   'n_slices': C4['slices'], 'form': 'fp64'},
+        'cpu_baseline': {'value': v, 'unit': 'macroparticle-turns/s',
+                         'cores': 1, 'kind': 'port', 'sample': sample},
+        'e2e': {'value': v, 'unit': 'macroparticle-turns/s',
+                'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }))
+
+
 # ------------------------------------------------------------ reference arm
 
 def run_reference(a, rank, world):
@@ -476,14 +767,21 @@ def main():
     ap.add_argument('--steps', type=int, default=400)
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', choices=['ours', 'reference'], default='ours')
-    ap.add_argument('--workload', choices=sorted(WORKLOADS), default='c2')
+    ap.add_argument('--workload', choices=sorted(WORKLOADS) + ['c4'],
+                    default='c2')
     ap.add_argument('--form', choices=['all', 'fp64', 'fp32'], default='all')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-autotune', dest='autotune', action='store_false',
+                    help='batched workload: skip timing the launch shapes')
     a = ap.parse_args()
+    a.steps_given = any(x == '--steps' or x.startswith('--steps=')
+                        for x in sys.argv[1:])
     a.warmup = max(3, a.warmup)
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     if a.impl == 'reference':
+        if a.workload == 'c4':
+            return run_reference_c4(a, rank, world)
         return run_reference(a, rank, world)
     if world > 1:
         import torch
@@ -491,7 +789,10 @@ def main():
         torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', rank)))
         dist.init_process_group('nccl')
         dist.barrier()
-    run_ours(a, rank, world)
+    if a.workload == 'c4':
+        run_batch(a, rank, world)
+    else:
+        run_ours(a, rank, world)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

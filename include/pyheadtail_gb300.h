@@ -237,6 +237,45 @@ typedef struct phk_wake_set {
     phk_wake_kick kick[PHK_MAX_KICKS];
 } phk_wake_set;
 
+/* ---- batched form: many bunches in one persistent launch ---------------
+ * No counterpart in the reference, which tracks one bunch per element
+ * call.  The coordinates of all bunches are concatenated in one set of six
+ * arrays; bunch b owns [offset_b, offset_b + n_b) with offset_b a multiple
+ * of 4.  Every bunch runs its own element program (its own chromaticity,
+ * detuning, RF parameters) and its own wake kicks; all bunches share one
+ * slicing (same cuts and slice count).
+ *
+ * A work unit is particles [start, end) of one bunch (start a multiple of
+ * 4).  CTA g of the persistent launch processes units cta_first[g] ..
+ * cta_first[g+1]-1 in order; consecutive units of one bunch accumulate
+ * into the partial column of the first of them.  Columns of bunch b are
+ * the range bunch_columns[b] .. bunch_columns[b+1]-1 of phk_batch_finalize.
+ * The kernel checks every table entry against the sizes below: a unit out
+ * of range is skipped and PHK_DEV_BAD_TABLE is stored in *status. */
+#define PHK_DEV_BAD_TABLE 2
+typedef struct phk_unit {
+    int64_t start;
+    int64_t end;
+    int32_t bunch;
+    int32_t column;
+} phk_unit;
+
+typedef struct phk_batch {
+    int32_t n_bunches;
+    int32_t n_units;
+    int32_t n_columns;
+    int32_t grid;               /* CTAs of the persistent launch */
+    int32_t threads;            /* 128, 256 or 512 threads per CTA */
+    int32_t reserved;
+    const phk_unit *units;      /* device [n_units] */
+    const int32_t *cta_first;   /* device [grid + 1] */
+    const phk_program *programs;      /* device [n_bunches] */
+    const phk_program *programs_host; /* the same programs, host memory */
+    const void *kicks;          /* device [n_bunches][n_kicks][n_slices],
+                                   coords dtype; NULL without pending kicks */
+    int32_t *status;            /* device word or NULL */
+} phk_batch;
+
 /* ---------------------------------------------------------------------- */
 
 int phk_abi_version(void);
@@ -294,6 +333,36 @@ int phk_slice_moments(const phk_slicer *slicer, const void *z, int64_t n,
                       int32_t dtype, const void *const *quantities, int32_t n_q,
                       int32_t pass, const double *means, double *sums,
                       int32_t *counts, void *stream);
+
+/* Batched fused pass (see phk_batch): per unit, the pending kicks of its
+ * bunch (tables batch->kicks; `pending` gives n_kicks, quad, target and the
+ * slicer, its kick[] pointers are ignored), the bunch's program, binning
+ * and per-slice sums into acc->partials[3][S][batch->n_columns]
+ * (acc->grid must equal n_columns).  acc may be NULL (no slicing). */
+int phk_track_batch(const phk_batch *batch, const phk_coords *coords,
+                    const phk_kick_set *pending, const phk_accum *acc,
+                    void *stream);
+
+/* Largest resident grid of phk_track_batch for a configuration: CTAs per
+ * SM at `threads` threads x SM count (sizes the persistent launch). */
+int phk_batch_max_grid(int32_t dtype, int32_t threads, int32_t n_slices,
+                       int32_t n_kicks);
+
+/* Per bunch b and slice s: fixed-order sum of the bunch's partial columns
+ * (bunch_columns: device int32[n_bunches + 1]) into counts[b*S + s],
+ * mean_x, mean_y (any may be NULL) and, if moments != NULL, the moment
+ * ring slot moments + b * moments_stride, laid out [3][S] as in
+ * phk_slice_finalize. */
+int phk_batch_finalize(const phk_accum *acc, int32_t n_bunches,
+                       const int32_t *bunch_columns, int32_t *counts,
+                       double *mean_x, double *mean_y, double *moments,
+                       int64_t moments_stride, void *stream);
+
+/* Wake convolution of every bunch: sets is a DEVICE array of n_bunches
+ * phk_wake_set (each with n_slices and at most n_kicks kicks); bunch b's
+ * convolution is the one phk_wake would compute for sets[b]. */
+int phk_wake_batch(const phk_wake_set *sets, int32_t n_bunches,
+                   int32_t n_slices, int32_t n_kicks, void *stream);
 
 /* Slicing pass that allocates nothing and takes no workspace; no
  * counterpart in the reference.  Same results as phk_track(empty program,

@@ -12,6 +12,7 @@ from . import _build
 
 PHK_F64, PHK_F32 = 0, 1
 PHK_DEV_TIMEOUT = 1
+PHK_DEV_BAD_TABLE = 2
 PHK_MAX_OPS = 12
 PHK_MAX_DETUNERS = 6
 PHK_MAX_POLY = 8
@@ -93,6 +94,21 @@ class WakeSet(ctypes.Structure):
                 ('kick', WakeKick * PHK_MAX_KICKS)]
 
 
+class Unit(ctypes.Structure):
+    _fields_ = [('start', ctypes.c_int64), ('end', ctypes.c_int64),
+                ('bunch', ctypes.c_int32), ('column', ctypes.c_int32)]
+
+
+class Batch(ctypes.Structure):
+    _fields_ = [('n_bunches', ctypes.c_int32), ('n_units', ctypes.c_int32),
+                ('n_columns', ctypes.c_int32), ('grid', ctypes.c_int32),
+                ('threads', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('units', ctypes.c_void_p), ('cta_first', ctypes.c_void_p),
+                ('programs', ctypes.c_void_p),
+                ('programs_host', ctypes.POINTER(Program)),
+                ('kicks', ctypes.c_void_p), ('status', ctypes.c_void_p)]
+
+
 class PhkError(RuntimeError):
     """A libphk entry point returned a non-zero status."""
 
@@ -117,6 +133,17 @@ SIGNATURES = {
                           ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
                           ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p, ctypes.c_void_p],
+    'phk_track_batch': [ctypes.POINTER(Batch), ctypes.POINTER(Coords),
+                        ctypes.POINTER(KickSet), ctypes.POINTER(Accum),
+                        ctypes.c_void_p],
+    'phk_batch_max_grid': [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                           ctypes.c_int32],
+    'phk_batch_finalize': [ctypes.POINTER(Accum), ctypes.c_int32,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                           ctypes.c_void_p],
+    'phk_wake_batch': [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                       ctypes.c_int32, ctypes.c_void_p],
     'phk_slice_noalloc': [ctypes.POINTER(Slicer), ctypes.POINTER(Coords),
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p],

@@ -275,4 +275,106 @@ int phk_slice_moments(const phk_slicer* slicer, const void* z, int64_t n,
                           sums, counts, (cudaStream_t)stream);
 }
 
+int phk_track_batch(const phk_batch* batch, const phk_coords* coords,
+                    const phk_kick_set* pending, const phk_accum* acc,
+                    void* stream) {
+    const char* who = "phk_track_batch";
+    if (!batch) return set_error(PHK_ENULL, "%s: batch is NULL", who);
+    const phk_batch& b = *batch;
+    if (b.n_bunches < 1)
+        return set_error(PHK_ESIZE, "%s: n_bunches %d < 1", who, b.n_bunches);
+    if (b.n_units < 0) return set_error(PHK_ESIZE, "%s: n_units < 0", who);
+    if (b.grid < 1) return set_error(PHK_ESIZE, "%s: grid %d < 1", who, b.grid);
+    if (b.threads != 128 && b.threads != 256 && b.threads != 512)
+        return set_error(PHK_EPARAM, "%s: threads %d is not 128, 256 or 512",
+                         who, b.threads);
+    if (!b.units || !b.cta_first || !b.programs || !b.programs_host)
+        return set_error(PHK_ENULL, "%s: units, cta_first or programs is NULL",
+                         who);
+    int r = check_coords(coords, who);
+    if (r) return r;
+    const void* p[6] = {coords->x, coords->xp, coords->y, coords->yp,
+                        coords->z, coords->dp};
+    for (int q = 0; q < 6; ++q)
+        if (reinterpret_cast<uintptr_t>(p[q]) % 16)
+            return set_error(PHK_EALIGN, "%s: coordinate %d not 16-byte "
+                             "aligned", who, q);
+    for (int i = 0; i < b.n_bunches; ++i)
+        if ((r = check_program(b.programs_host + i, who))) return r;
+    if (pending) {
+        if (!b.kicks)
+            return set_error(PHK_ENULL, "%s: pending kicks without tables", who);
+        phk_kick_set k = *pending;
+        for (int i = 0; i < k.n_kicks && i < PHK_MAX_KICKS; ++i)
+            k.kick[i] = b.kicks;
+        if ((r = check_kicks(&k, coords->dtype, who))) return r;
+        if ((size_t)k.n_kicks * k.slicer.n_slices * dsize(coords->dtype) >
+            48 * 1024)
+            return set_error(PHK_ESIZE, "%s: kick tables of one bunch exceed "
+                             "48 KB", who);
+    }
+    if (acc) {
+        if ((r = check_accum(acc, who))) return r;
+        if (b.n_columns < 1 || acc->grid != b.n_columns)
+            return set_error(PHK_EPARAM, "%s: acc->grid %d must equal "
+                             "n_columns %d >= 1", who, acc->grid, b.n_columns);
+    }
+    return launch_track_batch(batch, coords, pending, acc,
+                              (cudaStream_t)stream);
+}
+
+int phk_batch_max_grid(int32_t dtype, int32_t threads, int32_t n_slices,
+                       int32_t n_kicks) {
+    const char* who = "phk_batch_max_grid";
+    int r = check_dtype(dtype, who);
+    if (r) return r;
+    if (threads != 128 && threads != 256 && threads != 512)
+        return set_error(PHK_EPARAM, "%s: threads %d", who, threads);
+    if (n_slices < 1 || n_slices > PHK_MAX_SLICES)
+        return set_error(PHK_ESIZE, "%s: n_slices %d", who, n_slices);
+    if (n_kicks < 0 || n_kicks > PHK_MAX_KICKS)
+        return set_error(PHK_ESIZE, "%s: n_kicks %d", who, n_kicks);
+    const int g = batch_max_grid(dtype, threads, n_slices, n_kicks);
+    if (g < 1)
+        return set_error(PHK_ESIZE, "%s: configuration does not fit on an SM",
+                         who);
+    return g;
+}
+
+int phk_batch_finalize(const phk_accum* acc, int32_t n_bunches,
+                       const int32_t* bunch_columns, int32_t* counts,
+                       double* mean_x, double* mean_y, double* moments,
+                       int64_t moments_stride, void* stream) {
+    const char* who = "phk_batch_finalize";
+    if (!acc) return set_error(PHK_ENULL, "%s: acc is NULL", who);
+    int r = check_accum(acc, who);
+    if (r) return r;
+    if (n_bunches < 1)
+        return set_error(PHK_ESIZE, "%s: n_bunches %d < 1", who, n_bunches);
+    if (!bunch_columns)
+        return set_error(PHK_ENULL, "%s: bunch_columns is NULL", who);
+    if (moments && moments_stride < 3LL * acc->slicer.n_slices)
+        return set_error(PHK_EPARAM, "%s: moments_stride %lld < 3 * n_slices",
+                         who, (long long)moments_stride);
+    return launch_batch_finalize(acc, n_bunches, bunch_columns, counts, mean_x,
+                                 mean_y, moments, moments_stride, nullptr,
+                                 (cudaStream_t)stream);
+}
+
+int phk_wake_batch(const phk_wake_set* sets, int32_t n_bunches,
+                   int32_t n_slices, int32_t n_kicks, void* stream) {
+    const char* who = "phk_wake_batch";
+    if (!sets) return set_error(PHK_ENULL, "%s: sets is NULL", who);
+    if (n_bunches < 1)
+        return set_error(PHK_ESIZE, "%s: n_bunches %d < 1", who, n_bunches);
+    if (n_slices < 1 || n_slices > PHK_MAX_SLICES)
+        return set_error(PHK_ESIZE, "%s: n_slices %d outside [1, %d]", who,
+                         n_slices, PHK_MAX_SLICES);
+    if (n_kicks < 0 || n_kicks > PHK_MAX_KICKS)
+        return set_error(PHK_ESIZE, "%s: n_kicks %d", who, n_kicks);
+    if (n_kicks == 0) return PHK_OK;
+    return launch_wake_batch(sets, n_bunches, n_slices, n_kicks,
+                             (cudaStream_t)stream);
+}
+
 }  // extern "C"

@@ -38,4 +38,16 @@ int launch_moments(const phk_slicer* s, const void* z, int64_t n,
                    int32_t pass, const double* means, double* sums,
                    int32_t* counts, cudaStream_t stream);
 
+int launch_track_batch(const phk_batch* b, const phk_coords* c,
+                       const phk_kick_set* pk, const phk_accum* acc,
+                       cudaStream_t stream);
+int batch_max_grid(int32_t dtype, int32_t threads, int32_t n_slices,
+                   int32_t n_kicks);
+int launch_batch_finalize(const phk_accum* acc, int nb, const int32_t* bcols,
+                          int32_t* counts, double* mean_x, double* mean_y,
+                          double* moments, int64_t mstride, int32_t* status,
+                          cudaStream_t stream);
+int launch_wake_batch(const phk_wake_set* sets, int nb, int n_slices,
+                      int n_kicks, cudaStream_t stream);
+
 }  // namespace phk

@@ -1206,21 +1206,21 @@ int launch_track(const phk_program* prog, const phk_coords* c,
 // fixed-order merge of the per-CTA partials (one warp per slice)
 // ===================================================================
 
-__global__ void finalize_kernel(const double* __restrict__ P, int S, int G,
-                                int32_t* counts, double* mean_x,
-                                double* mean_y, double* moments) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= S) return;
-    const int s = warp;
+// Fixed-order sum of the partial columns [g0, g1) of slice s (P laid out
+// [3][S][G]) and the finalised outputs; all 32 lanes of the warp call it.
+__device__ __forceinline__ void merge_slice(const double* __restrict__ P,
+                                            int S, int G, int s, int g0,
+                                            int g1, int32_t* counts,
+                                            double* mean_x, double* mean_y,
+                                            double* moments, int lane) {
     const double* pc = P + (int64_t)s * G;
     const double* px = P + (int64_t)(S + s) * G;
     const double* py = P + (int64_t)(2 * S + s) * G;
     // four independent strided partial sums per lane (loads in flight),
     // combined in a fixed order: the result does not depend on timing
     double c[4] = {0, 0, 0, 0}, sx[4] = {0, 0, 0, 0}, sy[4] = {0, 0, 0, 0};
-    int g = lane;
-    for (; g + 96 < G; g += 128) {
+    int g = g0 + lane;
+    for (; g + 96 < g1; g += 128) {
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             c[u] += pc[g + 32 * u];
@@ -1228,7 +1228,7 @@ __global__ void finalize_kernel(const double* __restrict__ P, int S, int G,
             sy[u] += py[g + 32 * u];
         }
     }
-    for (; g < G; g += 32) {
+    for (; g < g1; g += 32) {
         c[0] += pc[g];
         sx[0] += px[g];
         sy[0] += py[g];
@@ -1258,6 +1258,15 @@ __global__ void finalize_kernel(const double* __restrict__ P, int S, int G,
     }
 }
 
+__global__ void finalize_kernel(const double* __restrict__ P, int S, int G,
+                                int32_t* counts, double* mean_x,
+                                double* mean_y, double* moments) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= S) return;
+    merge_slice(P, S, G, warp, 0, G, counts, mean_x, mean_y, moments, lane);
+}
+
 int launch_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
                     double* mean_y, double* moments, cudaStream_t st) {
     const int S = acc->slicer.n_slices;
@@ -1283,10 +1292,9 @@ struct WakeArgs {
 };
 
 // numpy path: one warp per (kick, target slice); lanes split the sources
-__global__ void wake_conv_kernel(const __grid_constant__ phk_wake_set w) {
+__device__ __forceinline__ void wake_conv_one(const phk_wake_set& w, int gw,
+                                              int lane) {
     const int S = w.n_slices;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
     const int k = gw / S;
     const int i = gw - k * S;
     if (k >= w.n_kicks) return;
@@ -1322,9 +1330,8 @@ __global__ void wake_conv_kernel(const __grid_constant__ phk_wake_set w) {
 }
 
 // dot-product path: one thread per (kick, target slice); coalesced over i
-__global__ void wake_dense_kernel(const __grid_constant__ phk_wake_set w) {
+__device__ __forceinline__ void wake_dense_one(const phk_wake_set& w, int t) {
     const int S = w.n_slices;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int k = t / S;
     const int i = t - k * S;
     if (k >= w.n_kicks) return;
@@ -1344,6 +1351,15 @@ __global__ void wake_dense_kernel(const __grid_constant__ phk_wake_set w) {
         reinterpret_cast<double*>(kk.out)[i] = r;
     else
         reinterpret_cast<float*>(kk.out)[i] = (float)r;
+}
+
+__global__ void wake_conv_kernel(const __grid_constant__ phk_wake_set w) {
+    wake_conv_one(w, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                  threadIdx.x & 31);
+}
+
+__global__ void wake_dense_kernel(const __grid_constant__ phk_wake_set w) {
+    wake_dense_one(w, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 int launch_wake(const phk_wake_set* w, cudaStream_t st) {
@@ -1437,6 +1453,373 @@ int launch_moments(const phk_slicer* sl, const void* z, int64_t n,
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_slice_moments launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+
+// ===================================================================
+// batched form: many bunches, one persistent launch
+// ===================================================================
+
+struct BatchArgs {
+    TrackArgs a;             // coordinates, masks, has_pk / has_acc, n_hist
+    const phk_unit* units;
+    const int32_t* cta_first;
+    const phk_program* programs;
+    const void* kicks;
+    int32_t* status;
+    int32_t n_bunches;
+    int32_t n_units;
+    int32_t n_columns;
+};
+
+constexpr size_t kProgSmem = (sizeof(phk_program) + 15) & ~(size_t)15;
+
+// Per CTA: its units in order.  When the bunch changes, the CTA's per-slice
+// sums of the previous bunch go to that bunch's partial column, and the new
+// bunch's program and kick tables are staged in shared memory.
+template <typename T, int VEC, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+batch_track_kernel(const __grid_constant__ phk_kick_set pk,
+                   const __grid_constant__ phk_accum acc, const BatchArgs b) {
+    using W = typename Hist<T>::Word;
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int TILE = THREADS * VEC;
+    const TrackArgs& a = b.a;
+    const int Sa = a.has_acc ? acc.slicer.n_slices : 0;
+    const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
+    const int nk = a.has_pk ? pk.n_kicks : 0;
+    phk_program* sprog = reinterpret_cast<phk_program*>(smem);
+    unsigned char* rest = smem + kProgSmem;
+    size_t off[9];
+    track_smem_layout<T>(Sa, Sp, a.n_hist, nk, 1, 0, TILE, off);
+    W* hsx = reinterpret_cast<W*>(rest + off[0]);
+    W* hsy = reinterpret_cast<W*>(rest + off[1]);
+    int* hcnt = reinterpret_cast<int*>(rest + off[2]);
+    T* eacc = reinterpret_cast<T*>(rest + off[3]);
+    T* epk = reinterpret_cast<T*>(rest + off[4]);
+    T* ktab = reinterpret_cast<T*>(rest + off[5]);
+    int* htag = reinterpret_cast<int*>(rest + off[6]);
+    const int tid = threadIdx.x;
+
+    if (a.has_acc) {
+        const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
+        for (int i = tid; i <= Sa; i += THREADS) stage_edge<T>(eacc, i, e[i]);
+        for (int i = tid; i < a.n_hist * Sa; i += THREADS) {
+            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
+            hcnt[i] = 0; htag[i] = 0;
+        }
+    }
+    if (a.has_pk) {
+        const T* e = reinterpret_cast<const T*>(pk.slicer.edges);
+        for (int i = tid; i <= Sp; i += THREADS) stage_edge<T>(epk, i, e[i]);
+    }
+
+    TrackCtx<T, VEC> cx;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) cx.cp[q] = reinterpret_cast<T*>(a.c[q]);
+    cx.ktab = ktab;
+    const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
+    cx.hx = hsx + h * Sa;
+    cx.hy = hsy + h * Sa;
+    cx.hc = hcnt + h * Sa;
+    cx.tag = htag + h * Sa;
+    cx.epoch = 0;
+    cx.shared_hist = a.n_hist < THREADS / 32;
+    __syncthreads();
+    if (a.has_pk) cx.bpk.init(epk, Sp, pk.slicer.negate);
+    if (a.has_acc) cx.bac.init(eacc, Sa, acc.slicer.negate);
+
+    int u0 = b.cta_first[blockIdx.x], u1 = b.cta_first[blockIdx.x + 1];
+    if (u0 < 0 || u1 > b.n_units || u0 > u1) {
+        if (tid == 0 && b.status) atomicMax(b.status, PHK_DEV_BAD_TABLE);
+        u0 = u1 = 0;
+    }
+    int cur = -1, col = -1;
+    // write the CTA's sums of the current bunch to its column, then zero
+    auto flush = [&]() {
+        __syncthreads();
+        for (int s = tid; s < Sa; s += THREADS) {
+            int c = hcnt[s];
+            for (int k = 1; k < a.n_hist; ++k) {
+                c += hcnt[k * Sa + s];
+                Hist<T>::merge(hsx + s, hsx + k * Sa + s);
+                Hist<T>::merge(hsy + s, hsy + k * Sa + s);
+            }
+            const int G = b.n_columns;
+            double* P = acc.partials;
+            P[(int64_t)s * G + col] = (double)c;
+            P[(int64_t)(Sa + s) * G + col] = Hist<T>::value(hsx + s);
+            P[(int64_t)(2 * Sa + s) * G + col] = Hist<T>::value(hsy + s);
+        }
+        __syncthreads();
+        for (int i = tid; i < a.n_hist * Sa; i += THREADS) {
+            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
+            hcnt[i] = 0; htag[i] = 0;
+        }
+    };
+    for (int u = u0; u < u1; ++u) {
+        const phk_unit U = b.units[u];
+        const bool ok = U.bunch >= 0 && U.bunch < b.n_bunches &&
+                        U.start >= 0 && U.start <= U.end && U.end <= a.n &&
+                        (U.start & 3) == 0 &&
+                        (!a.has_acc || (U.column >= 0 && U.column < b.n_columns));
+        if (!ok) {
+            if (tid == 0 && b.status) atomicMax(b.status, PHK_DEV_BAD_TABLE);
+            continue;
+        }
+        if (U.bunch != cur) {
+            if (cur >= 0 && a.has_acc) flush();
+            __syncthreads();       // the previous bunch's program is done
+            const int4* src = reinterpret_cast<const int4*>(b.programs + U.bunch);
+            int4* dst = reinterpret_cast<int4*>(sprog);
+            for (int i = tid; i < (int)(sizeof(phk_program) / 16); i += THREADS)
+                dst[i] = src[i];
+            if (a.has_pk) {
+                const T* kt = reinterpret_cast<const T*>(b.kicks) +
+                              (int64_t)U.bunch * nk * Sp;
+                for (int i = tid; i < nk * Sp; i += THREADS) ktab[i] = kt[i];
+            }
+            __syncthreads();
+            cur = U.bunch;
+            col = U.column;
+        }
+        TrackArgs ua = a;
+        ua.n = U.end;
+        for (int64_t base = U.start; base < U.end; base += TILE) {
+            const int64_t i0 = base + (int64_t)tid * VEC;
+            const bool full = i0 + VEC <= U.end;
+            Tile<T, VEC> t;
+            load_tile_plain<T, VEC>(ua, cx, t, i0, full);
+            run_tile<T, VEC>(*sprog, pk, acc, ua, cx, t, i0, full);
+        }
+    }
+    if (cur >= 0 && a.has_acc) flush();
+}
+
+static_assert(sizeof(phk_program) % 16 == 0, "program copied as int4");
+
+template <typename T>
+static size_t batch_smem(int Sa, int Sp, int nk, int threads, int* n_hist) {
+    const int tile = threads * (sizeof(T) == 8 ? 2 : 4);
+    size_t off[9];
+    const int warps = threads / 32;
+    // one private histogram copy per warp when it stays within 48 KB
+    int nh = Sa > 0 ? warps : 1;
+    size_t bytes = track_smem_layout<T>(Sa, Sp, nh, nk, 1, 0, tile, off);
+    if (bytes > 48 * 1024 && Sa > 0) {
+        nh = 1;
+        bytes = track_smem_layout<T>(Sa, Sp, nh, nk, 1, 0, tile, off);
+    }
+    *n_hist = nh;
+    return kProgSmem + bytes;
+}
+
+template <typename T, int VEC, int THREADS>
+static int batch_occupancy(size_t smem) {
+    static int done_for[64] = {0};
+    const DeviceInfo& d = device_info();
+    const int dev = d.device < 64 ? d.device : 63;
+    if (!done_for[dev]) {
+        cudaFuncAttributes fa;
+        size_t st = 0;
+        if (cudaFuncGetAttributes(&fa, batch_track_kernel<T, VEC, THREADS>) ==
+            cudaSuccess)
+            st = fa.sharedSizeBytes;
+        else
+            cudaGetLastError();
+        if (cudaFuncSetAttribute(batch_track_kernel<T, VEC, THREADS>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 d.max_smem_optin - (int)st) != cudaSuccess)
+            cudaGetLastError();
+        done_for[dev] = 1;
+    }
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, batch_track_kernel<T, VEC, THREADS>, THREADS, smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        nb = 0;
+    }
+    return nb;
+}
+
+template <typename T, int VEC, int THREADS>
+static int launch_batch_t(const phk_batch* bt, const phk_coords* c,
+                          const phk_kick_set* pk, const phk_accum* acc,
+                          int ld, int stm, cudaStream_t st) {
+    BatchArgs b;
+    memset(&b, 0, sizeof(b));
+    TrackArgs& a = b.a;
+    a.c[0] = c->x; a.c[1] = c->xp; a.c[2] = c->y;
+    a.c[3] = c->yp; a.c[4] = c->z; a.c[5] = c->dp;
+    a.n = c->n;
+    a.has_pk = pk != nullptr;
+    a.has_acc = acc != nullptr;
+    a.load_mask = ld;
+    a.store_mask = stm;
+    a.kicks_smem = 1;
+    a.cluster = 1;
+    a.stages = 0;
+    const int Sa = acc ? acc->slicer.n_slices : 0;
+    const int Sp = pk ? pk->slicer.n_slices : 0;
+    const int nk = pk ? pk->n_kicks : 0;
+    const size_t smem = batch_smem<T>(Sa, Sp, nk, THREADS, &a.n_hist);
+    if (batch_occupancy<T, VEC, THREADS>(smem) < 1)
+        return set_error(PHK_ESIZE, "phk_track_batch: %zu bytes of shared "
+                         "memory for %d + %d slices do not fit", smem, Sa, Sp);
+    b.units = bt->units;
+    b.cta_first = bt->cta_first;
+    b.programs = bt->programs;
+    b.kicks = bt->kicks;
+    b.status = bt->status;
+    b.n_bunches = bt->n_bunches;
+    b.n_units = bt->n_units;
+    b.n_columns = bt->n_columns;
+    static phk_kick_set zero_pk;
+    static phk_accum zero_acc;
+    batch_track_kernel<T, VEC, THREADS><<<bt->grid, THREADS, smem, st>>>(
+        pk ? *pk : zero_pk, acc ? *acc : zero_acc, b);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_track_batch launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+static void track_masks(const phk_program* prog, const phk_kick_set* pk,
+                        const phk_accum* acc, int* ld_out, int* stm_out) {
+    int ld, stm;
+    op_mask(prog, &ld, &stm);
+    if (pk) {
+        ld |= 1 << PHK_Z;
+        for (int k = 0; k < pk->n_kicks; ++k) {
+            ld |= 1 << pk->target[k];
+            stm |= 1 << pk->target[k];
+            if (pk->quad[k] >= 0) ld |= 1 << pk->quad[k];
+        }
+    }
+    if (acc) ld |= (1 << PHK_Z) | (1 << PHK_X) | (1 << PHK_Y);
+    ld |= stm;
+    *ld_out = ld;
+    *stm_out = stm;
+}
+
+int launch_track_batch(const phk_batch* bt, const phk_coords* c,
+                       const phk_kick_set* pk, const phk_accum* acc,
+                       cudaStream_t st) {
+    int ld = 0, stm = 0;
+    for (int i = 0; i < bt->n_bunches; ++i) {
+        int l, s;
+        track_masks(bt->programs_host + i, pk, acc, &l, &s);
+        ld |= l;
+        stm |= s;
+    }
+    if (c->dtype == PHK_F64) {
+        switch (bt->threads) {
+            case 128: return launch_batch_t<double, 2, 128>(bt, c, pk, acc, ld, stm, st);
+            case 512: return launch_batch_t<double, 2, 512>(bt, c, pk, acc, ld, stm, st);
+            default: return launch_batch_t<double, 2, 256>(bt, c, pk, acc, ld, stm, st);
+        }
+    }
+    switch (bt->threads) {
+        case 128: return launch_batch_t<float, 4, 128>(bt, c, pk, acc, ld, stm, st);
+        case 512: return launch_batch_t<float, 4, 512>(bt, c, pk, acc, ld, stm, st);
+        default: return launch_batch_t<float, 4, 256>(bt, c, pk, acc, ld, stm, st);
+    }
+}
+
+int batch_max_grid(int32_t dtype, int32_t threads, int32_t S, int32_t nk) {
+    int nh = 0;
+    int per_sm = 0;
+    if (dtype == PHK_F64) {
+        const size_t sm = batch_smem<double>(S, nk > 0 ? S : 0, nk, threads, &nh);
+        per_sm = threads == 128   ? batch_occupancy<double, 2, 128>(sm)
+                 : threads == 512 ? batch_occupancy<double, 2, 512>(sm)
+                                  : batch_occupancy<double, 2, 256>(sm);
+    } else {
+        const size_t sm = batch_smem<float>(S, nk > 0 ? S : 0, nk, threads, &nh);
+        per_sm = threads == 128   ? batch_occupancy<float, 4, 128>(sm)
+                 : threads == 512 ? batch_occupancy<float, 4, 512>(sm)
+                                  : batch_occupancy<float, 4, 256>(sm);
+    }
+    return per_sm * device_info().sm_count;
+}
+
+__global__ void batch_finalize_kernel(const double* __restrict__ P, int S,
+                                      int G, int nb,
+                                      const int32_t* __restrict__ bcols,
+                                      int32_t* counts, double* mean_x,
+                                      double* mean_y, double* moments,
+                                      int64_t mstride, int32_t* status) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int bunch = warp / S;
+    const int s = warp - bunch * S;
+    if (bunch >= nb) return;
+    int g0 = bcols[bunch], g1 = bcols[bunch + 1];
+    if (g0 < 0 || g1 > G || g0 > g1) {
+        if (lane == 0 && status) atomicMax(status, PHK_DEV_BAD_TABLE);
+        g0 = g1 = 0;
+    }
+    const int64_t o = (int64_t)bunch * S;
+    merge_slice(P, S, G, s, g0, g1, counts ? counts + o : nullptr,
+                mean_x ? mean_x + o : nullptr, mean_y ? mean_y + o : nullptr,
+                moments ? moments + bunch * mstride : nullptr, lane);
+}
+
+int launch_batch_finalize(const phk_accum* acc, int nb, const int32_t* bcols,
+                          int32_t* counts, double* mean_x, double* mean_y,
+                          double* moments, int64_t mstride, int32_t* status,
+                          cudaStream_t st) {
+    const int S = acc->slicer.n_slices;
+    const int64_t warps = (int64_t)nb * S;
+    const int threads = 256;
+    const int64_t blocks = (warps * 32 + threads - 1) / threads;
+    batch_finalize_kernel<<<(unsigned)blocks, threads, 0, st>>>(
+        acc->partials, S, acc->grid, nb, bcols, counts, mean_x, mean_y,
+        moments, mstride, status);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_batch_finalize launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+// one warp per (bunch, kick, target slice), numpy path; one thread per
+// (bunch, kick, target slice), dot-product path
+__global__ void batch_wake_kernel(const phk_wake_set* __restrict__ sets,
+                                  int nb, int S, int nk) {
+    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int per = nk * S;
+    const int64_t bunch = gw / per;
+    if (bunch >= nb) return;
+    const phk_wake_set& w = sets[bunch];
+    if (w.n_slices != S || w.n_kicks > nk || w.n_kicks < 0 ||
+        w.ring_len < 1 || w.head < 0 || w.head >= w.ring_len)
+        return;
+    const int r = (int)(gw - bunch * per);
+    wake_conv_one(w, r, lane);
+    // dense kicks: the warp's lanes take target slices r*32+lane of the
+    // warp-major numbering (warps [0, per/32] cover all nk*S targets)
+    const int t = r * 32 + lane;
+    if (t < per) wake_dense_one(w, t);
+}
+
+int launch_wake_batch(const phk_wake_set* sets, int nb, int S, int nk,
+                      cudaStream_t st) {
+    const int64_t warps = (int64_t)nb * nk * S;
+    const int threads = 256;
+    const int64_t blocks = (warps * 32 + threads - 1) / threads;
+    batch_wake_kernel<<<(unsigned)blocks, threads, 0, st>>>(sets, nb, S, nk);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_wake_batch launch: %s",
                          cudaGetErrorString(e));
     count_launches(1);
     return PHK_OK;
