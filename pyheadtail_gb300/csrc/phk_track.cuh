@@ -1,0 +1,1581 @@
+// The fused track kernel and the batched track kernel as templates, with
+// their launch helpers.  Included by the per-precision translation units
+// (phk_track_f32.cu, phk_track_f64.cu), which instantiate and launch them,
+// and by phk_kernels.cu for the host-side planning helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <cooperative_groups.h>
+
+#include <type_traits>
+
+#include "phk_device.cuh"
+#include "phk_internal.h"
+
+namespace phk {
+
+// ===================================================================
+// particle tiles: VEC particles per thread, one register array per
+// coordinate; every op below works op-major / particle-minor, reading its
+// parameters once per tile
+// ===================================================================
+
+template <typename T, int VEC>
+struct Tile {
+    T c[6][VEC];
+};
+
+// ===================================================================
+// element arithmetic, plain FP64 form (reference evaluation order)
+// ===================================================================
+
+// ChromaticitySegment detune: Horner with separately rounded steps, lowest
+// coefficient first, then the extra dp factors of the order > 3 path.
+__device__ __forceinline__ double chroma_poly(const double* c, int n, int z,
+                                             double dp) {
+    double r = c[n - 1];
+    for (int i = n - 2; i >= 0; --i) r = add(c[i], mul(r, dp));
+    r = mul(r, dp);
+    for (int i = 0; i < z; ++i) r = mul(r, dp);
+    return r;
+}
+
+__device__ __forceinline__ double amp_action(double c1, double twoa, double b,
+                                             double u, double up) {
+    // 1/2 * ((1+a^2)/b * u**2 + 2*a * u*up + b * up**2)
+    double s = mul(c1, mul(u, u));
+    if (twoa != 0.0) s = add(s, mul(mul(twoa, u), up));
+    s = add(s, mul(b, mul(up, up)));
+    return mul(0.5, s);
+}
+
+__device__ __forceinline__ double ij_term(double I, double J, bool hi,
+                                          bool hj, double cc, double ss) {
+    if (hi && hj) return add(mul(I, cc), mul(J, ss));
+    if (hi) return mul(I, cc);
+    if (hj) return mul(J, ss);
+    return 0.0;
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_transverse(const phk_op& op,
+                                              const phk_program& prog,
+                                              Tile<double, VEC>& t) {
+    const double* p = op.p;
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+    const double Dx0 = p[16], Dx1 = p[17], Dy0 = p[18], Dy1 = p[19];
+    double (&x)[VEC] = t.c[PHK_X];
+    double (&xp)[VEC] = t.c[PHK_XP];
+    double (&y)[VEC] = t.c[PHK_Y];
+    double (&yp)[VEC] = t.c[PHK_YP];
+    const double (&dp)[VEC] = t.c[PHK_DP];
+    if (!(op.flags & PHK_FLAG_DETUNED)) {
+        const double M00 = p[0], M01 = p[1], M10 = p[2], M11 = p[3];
+        const double M22 = p[4], M23 = p[5], M32 = p[6], M33 = p[7];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            if (disp) {
+                x[j] = sub(x[j], mul(Dx0, dp[j]));
+                y[j] = sub(y[j], mul(Dy0, dp[j]));
+            }
+            const double nx = add(mul(M00, x[j]), mul(M01, xp[j]));
+            const double nxp = add(mul(M10, x[j]), mul(M11, xp[j]));
+            const double ny = add(mul(M22, y[j]), mul(M23, yp[j]));
+            const double nyp = add(mul(M32, y[j]), mul(M33, yp[j]));
+            x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
+            if (disp) {
+                x[j] = add(x[j], mul(Dx1, dp[j]));
+                y[j] = add(y[j], mul(Dy1, dp[j]));
+            }
+        }
+        return;
+    }
+    double phx[VEC], phy[VEC];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) { phx[j] = p[20]; phy[j] = p[21]; }
+    for (int d = 0; d < op.det_count; ++d) {
+        const phk_detuner& dt = prog.det[op.det_begin + d];
+        if (dt.kind == PHK_DET_CHROMA) {
+            const int nx = dt.nx, ny = dt.ny, zx = dt.zx, zy = dt.zy;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                phx[j] = add(phx[j], chroma_poly(dt.c, nx, zx, dp[j]));
+                phy[j] = add(phy[j], chroma_poly(dt.c + 8, ny, zy, dp[j]));
+            }
+        } else {
+            const double ax = dt.c[0], ay = dt.c[1], axy = dt.c[2], ayx = dt.c[3];
+            const double c1x = dt.c[4], tax = dt.c[5], bx = dt.c[6];
+            const double c1y = dt.c[7], tay = dt.c[8], by = dt.c[9];
+            const double p0 = dt.c[10], ip0 = dt.c[11];
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                const double Jx = amp_action(c1x, tax, bx, x[j], xp[j]);
+                const double Jy = amp_action(c1y, tay, by, y[j], yp[j]);
+                phx[j] = add(phx[j], div_by(add(mul(ax, Jx), mul(axy, Jy)), p0, ip0));
+                phy[j] = add(phy[j], div_by(add(mul(ay, Jy), mul(ayx, Jx)), p0, ip0));
+            }
+        }
+    }
+    const double twopi = p[22];
+    const double phx0 = p[23], sx0 = p[24], cx0 = p[25];
+    const double phy0 = p[26], sy0 = p[27], cy0 = p[28];
+    const int m = op.ij_mask;
+    double I[8], J[8];
+    bool hI[8], hJ[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        I[e] = p[e]; J[e] = p[8 + e];
+        hI[e] = (m >> e) & 1; hJ[e] = (m >> (8 + e)) & 1;
+    }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        double sx, cx, sy, cy;
+        sincos_about(mul(phx[j], twopi), phx0, sx0, cx0, &sx, &cx);
+        sincos_about(mul(phy[j], twopi), phy0, sy0, cy0, &sy, &cy);
+        const double M00 = ij_term(I[0], J[0], hI[0], hJ[0], cx, sx);
+        const double M01 = ij_term(I[1], J[1], hI[1], hJ[1], cx, sx);
+        const double M10 = ij_term(I[2], J[2], hI[2], hJ[2], cx, sx);
+        const double M11 = ij_term(I[3], J[3], hI[3], hJ[3], cx, sx);
+        const double M22 = ij_term(I[4], J[4], hI[4], hJ[4], cy, sy);
+        const double M23 = ij_term(I[5], J[5], hI[5], hJ[5], cy, sy);
+        const double M32 = ij_term(I[6], J[6], hI[6], hJ[6], cy, sy);
+        const double M33 = ij_term(I[7], J[7], hI[7], hJ[7], cy, sy);
+        if (disp) {
+            x[j] = sub(x[j], mul(Dx0, dp[j]));
+            y[j] = sub(y[j], mul(Dy0, dp[j]));
+        }
+        const double nx = add(mul(M00, x[j]), mul(M01, xp[j]));
+        const double nxp = add(mul(M10, x[j]), mul(M11, xp[j]));
+        const double ny = add(mul(M22, y[j]), mul(M23, yp[j]));
+        const double nyp = add(mul(M32, y[j]), mul(M33, yp[j]));
+        x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
+        if (disp) {
+            x[j] = add(x[j], mul(Dx1, dp[j]));
+            y[j] = add(y[j], mul(Dy1, dp[j]));
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_drift(const phk_op& op,
+                                         Tile<double, VEC>& t) {
+    const double br = op.p[0], eta0 = op.p[1], L = op.p[2];
+    const bool shrink = op.flags & PHK_FLAG_SHRINK;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        const double z = t.c[PHK_Z][j];
+        const double zz = shrink ? mul(br, z) : z;
+        t.c[PHK_Z][j] = sub(zz, mul(mul(eta0, t.c[PHK_DP][j]), L));
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_rfkick(const phk_op& op,
+                                          Tile<double, VEC>& t) {
+    const double* p = op.p;
+    const int f = op.flags;
+    const double h = p[0], twopi = p[1], C = p[2], off = p[3], lock = p[4];
+    const double A = p[5], p0o = p[6], pinc = p[7], p0n = p[8];
+    const double Dx = p[9], Dy = p[10], iC = p[11], ip0n = p[12];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        double& dp = t.c[PHK_DP][j];
+        if (f & PHK_FLAG_DISPERSION) {
+            t.c[PHK_X][j] = sub(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = sub(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+        double phi = mul(h, div_by(mul(twopi, t.c[PHK_Z][j]), C, iC));
+        if (f & PHK_FLAG_PHI_OFFSET) phi = add(phi, off);
+        if (f & PHK_FLAG_PHI_LOCK) phi = add(phi, lock);
+        double s = mul(A, sin(phi));
+        if (f & PHK_FLAG_P_INC) s = sub(s, pinc);
+        dp = div_by(add(mul(dp, p0o), s), p0n, ip0n);
+        if (f & PHK_FLAG_DISPERSION) {
+            t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_linear_long(const phk_op& op,
+                                               Tile<double, VEC>& t) {
+    const double* p = op.p;
+    const double cs = p[0], sn = p[1], lf = p[2], Dx = p[3], Dy = p[4];
+    const double ilf = p[5];
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        double& z = t.c[PHK_Z][j];
+        double& dp = t.c[PHK_DP][j];
+        if (disp) {
+            t.c[PHK_X][j] = sub(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = sub(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+        const double z0 = z, dp0 = dp;
+        z = sub(mul(z0, cs), mul(mul(lf, dp0), sn));
+        dp = add(mul(dp0, cs), mul(div_by(z0, lf, ilf), sn));
+        if (disp) {
+            t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_scale(const phk_op& op,
+                                         Tile<double, VEC>& t) {
+    const double f = op.p[0];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) t.c[q][j] = mul(t.c[q][j], f);
+}
+
+// ===================================================================
+// element arithmetic, FP32 precision form (parameters packed as floats)
+// ===================================================================
+
+__device__ __forceinline__ float chroma_poly_f32(const float* c, int n, int z,
+                                                 float dp) {
+    float r = c[n - 1];
+    for (int i = n - 2; i >= 0; --i) r = fmaf(r, dp, c[i]);
+    r *= dp;
+    for (int i = 0; i < z; ++i) r *= dp;
+    return r;
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_transverse(const phk_op& op,
+                                              const phk_program& prog,
+                                              Tile<float, VEC>& t) {
+    const float* p = reinterpret_cast<const float*>(op.p);
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+    const float Dx0 = p[32], Dx1 = p[33], Dy0 = p[34], Dy1 = p[35];
+    float (&x)[VEC] = t.c[PHK_X];
+    float (&xp)[VEC] = t.c[PHK_XP];
+    float (&y)[VEC] = t.c[PHK_Y];
+    float (&yp)[VEC] = t.c[PHK_YP];
+    const float (&dp)[VEC] = t.c[PHK_DP];
+    float M[8][VEC];
+    if (op.flags & PHK_FLAG_DETUNED) {
+        float dqx[VEC], dqy[VEC];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) { dqx[j] = 0.f; dqy[j] = 0.f; }
+        for (int d = 0; d < op.det_count; ++d) {
+            const phk_detuner& dt = prog.det[op.det_begin + d];
+            const float* c = reinterpret_cast<const float*>(dt.c);
+            if (dt.kind == PHK_DET_CHROMA) {
+                const int nx = dt.nx, ny = dt.ny, zx = dt.zx, zy = dt.zy;
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) {
+                    dqx[j] += chroma_poly_f32(c, nx, zx, dp[j]);
+                    dqy[j] += chroma_poly_f32(c + 8, ny, zy, dp[j]);
+                }
+            } else {
+                // c = dapp_x/p0, dapp_y/p0, dapp_xy/p0, dapp_yx/p0,
+                //     (1+ax^2)/bx, 2ax, bx, (1+ay^2)/by, 2ay, by
+                const float ax = c[0], ay = c[1], axy = c[2], ayx = c[3];
+                const float c1x = c[4], tax = c[5], bx = c[6];
+                const float c1y = c[7], tay = c[8], by = c[9];
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) {
+                    const float Jx = 0.5f * fmaf(bx * xp[j], xp[j],
+                                                 fmaf(tax * x[j], xp[j], c1x * x[j] * x[j]));
+                    const float Jy = 0.5f * fmaf(by * yp[j], yp[j],
+                                                 fmaf(tay * y[j], yp[j], c1y * y[j] * y[j]));
+                    dqx[j] += fmaf(ax, Jx, axy * Jy);
+                    dqy[j] += fmaf(ay, Jy, ayx * Jx);
+                }
+            }
+        }
+        const float qxh = p[16], qxl = p[17], qyh = p[18], qyl = p[19];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            float sx, cx, sy, cy;
+            sincos_turns(qxh, qxl, dqx[j], &sx, &cx);
+            sincos_turns(qyh, qyl, dqy[j], &sy, &cy);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                M[e][j] = fmaf(p[e], cx, p[8 + e] * sx);
+                M[4 + e][j] = fmaf(p[4 + e], cy, p[12 + e] * sy);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) M[e][j] = p[e];
+    }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        if (disp) {
+            x[j] = fmaf(-Dx0, dp[j], x[j]);
+            y[j] = fmaf(-Dy0, dp[j], y[j]);
+        }
+        const float nx = fmaf(M[0][j], x[j], M[1][j] * xp[j]);
+        const float nxp = fmaf(M[2][j], x[j], M[3][j] * xp[j]);
+        const float ny = fmaf(M[4][j], y[j], M[5][j] * yp[j]);
+        const float nyp = fmaf(M[6][j], y[j], M[7][j] * yp[j]);
+        x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
+        if (disp) {
+            x[j] = fmaf(Dx1, dp[j], x[j]);
+            y[j] = fmaf(Dy1, dp[j], y[j]);
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_drift(const phk_op& op,
+                                         Tile<float, VEC>& t) {
+    const float* p = reinterpret_cast<const float*>(op.p);
+    const float br = p[0], etaL = p[1];
+    const bool shrink = op.flags & PHK_FLAG_SHRINK;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        // z = beta_ratio * z - (eta0 * L) * dp
+        const float z = t.c[PHK_Z][j];
+        t.c[PHK_Z][j] = fmaf(-etaL, t.c[PHK_DP][j], shrink ? br * z : z);
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_rfkick(const phk_op& op,
+                                          Tile<float, VEC>& t) {
+    // p: h/C (hi, lo) turns per metre, (phi_offset+phi_lock)/2pi (hi, lo),
+    //    A/p0_new, p0_old/p0_new, p_inc/p0_new, -, D_x, D_y
+    const float* p = reinterpret_cast<const float*>(op.p);
+    const float mh = p[0], ml = p[1], oh = p[2], ol = p[3];
+    const float A = p[4], ratio = p[5], pinc = p[6], Dx = p[8], Dy = p[9];
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        float& dp = t.c[PHK_DP][j];
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(-Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
+        }
+        const float s = sin_turns_of_product(t.c[PHK_Z][j], mh, ml, oh, ol);
+        dp = fmaf(A, s, fmaf(dp, ratio, -pinc));
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_linear_long(const phk_op& op,
+                                               Tile<float, VEC>& t) {
+    // p: cos, sin, longfac, 1/longfac, D_x, D_y
+    const float* p = reinterpret_cast<const float*>(op.p);
+    const float cs = p[0], sn = p[1], lf = p[2], ilf = p[3];
+    const float Dx = p[4], Dy = p[5];
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        float& z = t.c[PHK_Z][j];
+        float& dp = t.c[PHK_DP][j];
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(-Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
+        }
+        const float z0 = z, dp0 = dp;
+        z = fmaf(z0, cs, -(lf * dp0) * sn);
+        dp = fmaf(dp0, cs, (z0 * ilf) * sn);
+        if (disp) {
+            t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
+            t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);
+        }
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_scale(const phk_op& op,
+                                         Tile<float, VEC>& t) {
+    const float f = reinterpret_cast<const float*>(op.p)[0];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) t.c[q][j] *= f;
+}
+
+// one dispatch per op per tile (uniform across the CTA)
+template <typename T, int VEC>
+__device__ __forceinline__ void run_program(const phk_program& prog,
+                                            Tile<T, VEC>& t) {
+    for (int o = 0; o < prog.n_ops; ++o) {
+        const phk_op& op = prog.op[o];
+        switch (op.kind) {
+            case PHK_OP_TRANSVERSE: op_transverse<VEC>(op, prog, t); break;
+            case PHK_OP_DRIFT: op_drift<VEC>(op, t); break;
+            case PHK_OP_RF_KICK: op_rfkick<VEC>(op, t); break;
+            case PHK_OP_LINEAR_LONG: op_linear_long<VEC>(op, t); break;
+            case PHK_OP_SCALE_TRANS: op_scale<VEC>(op, t); break;
+            default: break;
+        }
+    }
+}
+
+// Element sequences with a compile-time shape: the op parameters are then
+// read at fixed offsets of the kernel's parameter block (constant-bank
+// operands) instead of through a per-tile dispatch loop.
+enum TrackShape {
+    SHAPE_GENERIC = 0,   // any program: run_program's loop
+    SHAPE_NONE = 1,      // no ops (slicing / kicks only)
+    SHAPE_T = 2,         // one transverse segment
+    SHAPE_T_RF = 3,      // transverse, drift, RF kick, drift (RFSystems)
+    SHAPE_T_LIN = 4,     // transverse, linear longitudinal map
+};
+
+template <typename T, int VEC, int SHAPE>
+__device__ __forceinline__ void run_program_shape(const phk_program& prog,
+                                                  Tile<T, VEC>& t) {
+    if constexpr (SHAPE == SHAPE_NONE) {
+        return;
+    } else if constexpr (SHAPE == SHAPE_T) {
+        op_transverse<VEC>(prog.op[0], prog, t);
+    } else if constexpr (SHAPE == SHAPE_T_RF) {
+        op_transverse<VEC>(prog.op[0], prog, t);
+        op_drift<VEC>(prog.op[1], t);
+        op_rfkick<VEC>(prog.op[2], t);
+        op_drift<VEC>(prog.op[3], t);
+    } else if constexpr (SHAPE == SHAPE_T_LIN) {
+        op_transverse<VEC>(prog.op[0], prog, t);
+        op_linear_long<VEC>(prog.op[1], t);
+    } else {
+        run_program<T, VEC>(prog, t);
+    }
+}
+
+// ===================================================================
+// per-slice accumulation in shared memory, deterministic
+//   Each warp owns a private histogram (count, sum x, sum y per slice).
+//   Lanes of a warp holding the same slice are found with match.any; they
+//   update the bin one after the other in lane order (rank steps separated
+//   by __syncwarp), so no atomics are needed and the sums do not depend on
+//   scheduling.  FP64 form: plain double sums.  FP32 form: Kahan (1965)
+//   compensated float sums, one (sum, compensation) float2 per bin.
+//   When the per-warp copies do not fit, warps share one histogram and the
+//   updates fall back to atomics (FP64 form only needs that above ~500
+//   slices; the FP32 form always fits up to PHK_MAX_SLICES / 8 warps).
+// ===================================================================
+
+template <typename T>
+struct Hist;
+
+template <>
+struct Hist<double> {
+    using Word = double;
+    static __device__ __forceinline__ void zero(Word* w) { *w = 0.0; }
+    static __device__ __forceinline__ void add(Word* w, double v) {
+        *w = ::phk::add(*w, v);
+    }
+    static __device__ __forceinline__ void add_atomic(Word* w, double v) {
+        atomicAdd(w, v);
+    }
+    static __device__ __forceinline__ void merge(Word* dst, const Word* src) {
+        *dst = ::phk::add(*dst, *src);
+    }
+    static __device__ __forceinline__ double value(const Word* w) { return *w; }
+};
+
+template <>
+struct Hist<float> {
+    using Word = float2;  // x: running sum, y: Kahan compensation
+    static __device__ __forceinline__ void zero(Word* w) {
+        *w = make_float2(0.f, 0.f);
+    }
+    static __device__ __forceinline__ void add(Word* w, float v) {
+        float2 a = *w;
+        const float yk = v - a.y;
+        const float tk = a.x + yk;
+        a.y = (tk - a.x) - yk;
+        a.x = tk;
+        *w = a;
+    }
+    static __device__ __forceinline__ void add_atomic(Word* w, float v) {
+        atomicAdd(&w->x, v);
+    }
+    static __device__ __forceinline__ void merge(Word* dst, const Word* src) {
+        const float2 b = *src;
+        add(dst, b.x - b.y);
+    }
+    static __device__ __forceinline__ double value(const Word* w) {
+        const float2 a = *w;
+        return (double)(a.x - a.y);
+    }
+};
+
+// All 32 lanes of the warp must call this together; s < 0 means "no bin".
+// Lanes of a warp that hold the same slice are serialised by bids: in each
+// round every pending lane bids atomicMax(tag[s], epoch << 5 | lane) on the
+// warp's private tag array; the standing bid (the highest pending lane of
+// that slice) updates the bin with plain loads and stores.  A bin is thus
+// always updated in descending lane order: the sums are deterministic.
+template <typename T>
+__device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
+                                                typename Hist<T>::Word* hx,
+                                                typename Hist<T>::Word* hy,
+                                                int* hc, int* tag,
+                                                unsigned& epoch,
+                                                bool shared_hist) {
+    if (shared_hist) {
+        if (s >= 0) {
+            atomicAdd(hc + s, 1);
+            Hist<T>::add_atomic(hx + s, vx);
+            Hist<T>::add_atomic(hy + s, vy);
+        }
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    bool pending = s >= 0;
+    while (__any_sync(0xffffffffu, pending)) {
+        ++epoch;
+        const int bid = (int)((epoch << 5) | (unsigned)lane);
+        if (pending) atomicMax(tag + s, bid);
+        __syncwarp();
+        if (pending && tag[s] == bid) {
+            hc[s] += 1;
+            Hist<T>::add(hx + s, vx);
+            Hist<T>::add(hy + s, vy);
+            pending = false;
+        }
+        __syncwarp();
+    }
+}
+
+// ===================================================================
+// the fused track kernel
+// ===================================================================
+
+template <typename T, int VEC>
+struct VecIO;
+template <>
+struct VecIO<double, 2> {
+    static __device__ __forceinline__ void ld(const double* p, double (&o)[2]) {
+        const double2 t = *reinterpret_cast<const double2*>(p);
+        o[0] = t.x; o[1] = t.y;
+    }
+    static __device__ __forceinline__ void st(double* p, const double (&v)[2]) {
+        *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    }
+};
+template <>
+struct VecIO<float, 2> {
+    static __device__ __forceinline__ void ld(const float* p, float (&o)[2]) {
+        const float2 t = *reinterpret_cast<const float2*>(p);
+        o[0] = t.x; o[1] = t.y;
+    }
+    static __device__ __forceinline__ void st(float* p, const float (&v)[2]) {
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    }
+};
+template <>
+struct VecIO<float, 4> {
+    static __device__ __forceinline__ void ld(const float* p, float (&o)[4]) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+    }
+    static __device__ __forceinline__ void st(float* p, const float (&v)[4]) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <typename T>
+struct VecIO<T, 1> {
+    static __device__ __forceinline__ void ld(const T* p, T (&o)[1]) { o[0] = *p; }
+    static __device__ __forceinline__ void st(T* p, const T (&v)[1]) { *p = v[0]; }
+};
+
+struct TrackArgs {
+    void* c[6];
+    int64_t n;
+    int64_t n_tiles;
+    int32_t has_pk;
+    int32_t has_acc;
+    int32_t load_mask;
+    int32_t store_mask;
+    int32_t n_hist;      // histogram copies per CTA (1 or warps per CTA)
+    int32_t kicks_smem;  // kick tables staged in shared memory
+    int32_t cluster;     // CTAs per thread-block cluster (accumulation)
+    int32_t stages;      // TMA ring stages (0: plain loads)
+    int32_t kick_comb;   // kicks staged as one summed table per target
+    int32_t comb_slot[3];  // table of target xp, yp, dp (-1: none)
+};
+
+template <typename T>
+__device__ __forceinline__ T tadd(T a, T b);
+template <>
+__device__ __forceinline__ double tadd<double>(double a, double b) { return add(a, b); }
+template <>
+__device__ __forceinline__ float tadd<float>(float a, float b) { return a + b; }
+template <typename T>
+__device__ __forceinline__ T tmul(T a, T b);
+template <>
+__device__ __forceinline__ double tmul<double>(double a, double b) { return mul(a, b); }
+template <>
+__device__ __forceinline__ float tmul<float>(float a, float b) { return a * b; }
+
+// shared memory layout, in this order (every region 16-byte aligned):
+//   histogram words  [3][n_hist][Sa]   (sum x, sum y as Hist<T>::Word; count
+//                                       as int in the third region)
+//   accumulation edges [Sa + 1] T, pending-kick edges [Sp + 1] T,
+//   kick tables [n_kicks][Sp] T (when staged), bid tags [n_hist][Sa] int,
+//   TMA ring [stages][6][tile] T, one mbarrier per stage
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+template <typename T>
+__host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
+                                                    int n_kicks, int kicks_smem,
+                                                    int stages, int tile,
+                                                    size_t* off) {
+    size_t b = 0;
+    off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x words
+    off[1] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum y words
+    off[2] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // count
+    off[3] = b; b = align16(b + sizeof(T) * (Sa > 0 ? Sa + 1 : 0));
+    off[4] = b; b = align16(b + sizeof(T) * (Sp > 0 ? Sp + 1 : 0));
+    off[5] = b; b = align16(b + (kicks_smem ? sizeof(T) * (size_t)n_kicks * Sp : 0));
+    off[6] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // bid tags
+    off[7] = b; b = align16(b + (size_t)stages * 6 * tile * sizeof(T));
+    off[8] = b; b = align16(b + (size_t)8 * stages);         // mbarriers
+    return b;
+}
+
+// Exact slice lookup against a staged edge table.  FP32: the float edges
+// themselves.  FP64: order-preserving int64 keys of the edges, so that the
+// lookup needs no FP64 instruction (the first estimate is FP32).
+template <typename T>
+__device__ __forceinline__ void stage_edge(T* dst, int i, T e);
+template <>
+__device__ __forceinline__ void stage_edge<float>(float* dst, int i, float e) {
+    dst[i] = e;
+}
+template <>
+__device__ __forceinline__ void stage_edge<double>(double* dst, int i,
+                                                   double e) {
+    reinterpret_cast<long long*>(dst)[i] = order_key(e);
+}
+
+template <typename T>
+struct Bins;
+template <>
+struct Bins<float> {
+    const float* e;
+    int S, neg;
+    float tail, iw, e0, eS;
+    __device__ __forceinline__ void init(const float* edges, int n, int negate) {
+        e = edges; S = n; neg = negate;
+        e0 = e[0]; eS = e[S];
+        tail = e0;
+        const float span = eS - e0;
+        iw = span > 0.f ? (float)S / span : 0.f;
+    }
+    // Exact slice of VEC particles: every estimate and both bracketing
+    // edges are issued before any correction, so the shared-memory loads of
+    // the VEC lookups overlap.  The corrections walk at most to the table
+    // ends (e0 <= zz < eS holds inside), so no access leaves e[0..S].
+    template <int VEC>
+    __device__ __forceinline__ void index_vec(const float (&z)[VEC],
+                                              int (&out)[VEC]) const {
+        float zz[VEC], lo[VEC], hi[VEC];
+        int k[VEC];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            zz[j] = neg ? -z[j] : z[j];
+            int kk = (int)((zz[j] - tail) * iw);
+            k[j] = kk < 0 ? 0 : (kk > S - 1 ? S - 1 : kk);
+        }
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) { lo[j] = e[k[j]]; hi[j] = e[k[j] + 1]; }
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            if (!(zz[j] >= e0) || !(zz[j] < eS)) { out[j] = -1; continue; }
+            int kk = k[j];
+            float l = lo[j], h = hi[j];
+            while (zz[j] < l) { --kk; h = l; l = e[kk]; }
+            while (zz[j] >= h) { ++kk; h = e[kk + 1]; }
+            out[j] = kk;
+        }
+    }
+    __device__ __forceinline__ int index(float z) const {
+        float zv[1] = {z};
+        int o[1];
+        index_vec<1>(zv, o);
+        return o[0];
+    }
+};
+template <>
+struct Bins<double> {
+    const long long* k;
+    int S, neg;
+    float tail, iw;
+    long long k0, kS;
+    __device__ __forceinline__ void init(const double* edges, int n, int negate) {
+        k = reinterpret_cast<const long long*>(edges); S = n; neg = negate;
+        k0 = k[0]; kS = k[S];
+        // undo the key map for the two end edges (keys of finite doubles)
+        const float lo = approx_float(key_to_double(k0));
+        const float hi = approx_float(key_to_double(kS));
+        tail = lo;
+        const float span = hi - lo;
+        iw = span > 0.f ? (float)S / span : 0.f;
+    }
+    template <int VEC>
+    __device__ __forceinline__ void index_vec(const double (&z)[VEC],
+                                              int (&out)[VEC]) const {
+        long long kz[VEC], lo[VEC], hi[VEC];
+        int b[VEC];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const double zz = neg ? -z[j] : z[j];
+            kz[j] = order_key(zz);
+            int kk = (int)((approx_float(zz) - tail) * iw);
+            b[j] = kk < 0 ? 0 : (kk > S - 1 ? S - 1 : kk);
+        }
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) { lo[j] = k[b[j]]; hi[j] = k[b[j] + 1]; }
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            if (kz[j] < k0 || kz[j] >= kS) { out[j] = -1; continue; }
+            int kk = b[j];
+            long long l = lo[j], h = hi[j];
+            while (kz[j] < l) { --kk; h = l; l = k[kk]; }
+            while (kz[j] >= h) { ++kk; h = k[kk + 1]; }
+            out[j] = kk;
+        }
+    }
+    __device__ __forceinline__ int index(double z) const {
+        double zv[1] = {z};
+        int o[1];
+        index_vec<1>(zv, o);
+        return o[0];
+    }
+};
+
+// Per-CTA state shared by the tile loops of the track kernel.
+template <typename T, int VEC>
+struct TrackCtx {
+    using W = typename Hist<T>::Word;
+    T* cp[6];
+    Bins<T> bpk, bac;
+    const T* ktab;
+    W* hx;
+    W* hy;
+    int* hc;
+    int* tag;
+    unsigned epoch;
+    bool shared_hist;
+};
+
+// One tile of VEC particles per thread, already in registers: pending
+// kicks, element program, slice accumulation; then the stores.  All threads
+// of the CTA call this together (the accumulation is warp-synchronous);
+// lanes whose particles are past the end pass live = false.
+template <typename T, int VEC, int SHAPE, bool FULL>
+__device__ __forceinline__ void run_tile(const phk_program& prog,
+                                         const phk_kick_set& pk,
+                                         const phk_accum& acc,
+                                         const TrackArgs& a,
+                                         TrackCtx<T, VEC>& cx, Tile<T, VEC>& t,
+                                         int64_t i0, bool full) {
+    const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
+    const int nk = a.has_pk ? pk.n_kicks : 0;
+    // 1. wake kicks of the previous WakeField.track, in kick order
+    if (a.has_pk) {
+        int sl[VEC];
+        cx.bpk.index_vec(t.c[PHK_Z], sl);
+        if (a.kick_comb) {
+            // FP32 form, dipolar kicks only: one table per target, the
+            // kicks of that target summed at staging
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                const int s = sl[j];
+                if (s < 0 || (!FULL && i0 + j >= a.n)) continue;
+                if (a.comb_slot[0] >= 0)
+                    t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], cx.ktab[a.comb_slot[0] * Sp + s]);
+                if (a.comb_slot[1] >= 0)
+                    t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], cx.ktab[a.comb_slot[1] * Sp + s]);
+                if (a.comb_slot[2] >= 0)
+                    t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], cx.ktab[a.comb_slot[2] * Sp + s]);
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                const int s = sl[j];
+                if (s < 0 || (!FULL && i0 + j >= a.n)) continue;
+                const T kx = t.c[PHK_X][j], ky = t.c[PHK_Y][j];
+                for (int k = 0; k < nk; ++k) {
+                    T val = a.kicks_smem
+                                ? cx.ktab[k * Sp + s]
+                                : __ldg(reinterpret_cast<const T*>(pk.kick[k]) + s);
+                    const int qd = pk.quad[k];
+                    if (qd == PHK_X) val = tmul<T>(val, kx);
+                    else if (qd == PHK_Y) val = tmul<T>(val, ky);
+                    const int tg = pk.target[k];
+                    if (tg == PHK_XP) t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], val);
+                    else if (tg == PHK_YP) t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], val);
+                    else t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], val);
+                }
+            }
+        }
+    }
+    // 2. element program
+    run_program_shape<T, VEC, SHAPE>(prog, t);
+    // 3. slice accumulation
+    if (a.has_acc) {
+        int sl[VEC];
+        cx.bac.index_vec(t.c[PHK_Z], sl);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const bool live = FULL || i0 + j < a.n;
+            const int s = live ? sl[j] : -1;
+            if (acc.idx_out && live)
+                acc.idx_out[i0 + j] =
+                    s >= 0 ? s
+                           : outside_index((double)t.c[PHK_Z][j],
+                                           acc.slicer.tail, acc.slicer.width);
+            warp_accumulate<T>(s, t.c[PHK_X][j], t.c[PHK_Y][j], cx.hx, cx.hy,
+                               cx.hc, cx.tag, cx.epoch, cx.shared_hist);
+        }
+    }
+    // 4. stores of the coordinates the tile changed
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        if (!((a.store_mask >> q) & 1)) continue;
+        if (FULL || full) {
+            VecIO<T, VEC>::st(cx.cp[q] + i0, t.c[q]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j)
+                if (i0 + j < a.n) cx.cp[q][i0 + j] = t.c[q][j];
+        }
+    }
+}
+
+template <typename T, int VEC>
+__device__ __forceinline__ void load_tile_plain(const TrackArgs& a,
+                                                const TrackCtx<T, VEC>& cx,
+                                                Tile<T, VEC>& t, int64_t i0,
+                                                bool full) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        if (!((a.load_mask >> q) & 1)) {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
+            continue;
+        }
+        if (full) {
+            VecIO<T, VEC>::ld(cx.cp[q] + i0, t.c[q]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j)
+                t.c[q][j] = (i0 + j < a.n) ? cx.cp[q][i0 + j] : T(0);
+        }
+    }
+}
+
+// FP32 single-bunch kernel: particles per thread, resident CTAs per SM it
+// is compiled for (register cap) and the shared memory a CTA may plan for
+constexpr int kF32Vec = 2;
+constexpr int kF32MinBlocks = 4;
+constexpr size_t kF32SmemBudget = 54 * 1024;
+constexpr size_t kF64SmemBudget = 112 * 1024;
+
+// polls of one mbarrier phase before a kernel gives up (order of a second)
+constexpr unsigned kWaitLimit = 1u << 22;
+
+// FP32 launches aim at four resident CTAs per SM (<= 64 registers), FP64
+// ones at two (<= 128 registers; the FP64 pipe needs the warps to hide
+// its latency)
+template <typename T, int VEC, int SHAPE>
+__global__ void __launch_bounds__(kTrackThreads, sizeof(T) == 4 ? kF32MinBlocks : 2)
+track_kernel(const __grid_constant__ phk_program prog,
+             const __grid_constant__ phk_kick_set pk,
+             const __grid_constant__ phk_accum acc, const TrackArgs a) {
+    using W = typename Hist<T>::Word;
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int TILE = kTrackThreads * VEC;
+    const int Sa = a.has_acc ? acc.slicer.n_slices : 0;
+    const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
+    const int nk = a.has_pk ? pk.n_kicks : 0;
+    size_t off[9];
+    track_smem_layout<T>(Sa, Sp, a.n_hist, nk, a.kicks_smem, a.stages, TILE,
+                         off);
+    W* hsx = reinterpret_cast<W*>(smem + off[0]);
+    W* hsy = reinterpret_cast<W*>(smem + off[1]);
+    int* hcnt = reinterpret_cast<int*>(smem + off[2]);
+    T* eacc = reinterpret_cast<T*>(smem + off[3]);
+    T* epk = reinterpret_cast<T*>(smem + off[4]);
+    T* ktab = reinterpret_cast<T*>(smem + off[5]);
+    int* htag = reinterpret_cast<int*>(smem + off[6]);
+    T* ring = reinterpret_cast<T*>(smem + off[7]);
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + off[8]);
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        s_fail = 0;
+        for (int st = 0; st < a.stages; ++st) mbar_init(bars + st, 1);
+        if (a.stages > 0) mbar_fence_init();
+    }
+    if (a.has_acc) {
+        const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
+        for (int i = tid; i <= Sa; i += blockDim.x) stage_edge<T>(eacc, i, e[i]);
+        for (int i = tid; i < a.n_hist * Sa; i += blockDim.x) {
+            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
+            hcnt[i] = 0; htag[i] = 0;
+        }
+    }
+    if (a.has_pk) {
+        const T* e = reinterpret_cast<const T*>(pk.slicer.edges);
+        for (int i = tid; i <= Sp; i += blockDim.x) stage_edge<T>(epk, i, e[i]);
+        if (a.kick_comb) {
+            for (int i = tid; i < Sp; i += blockDim.x) {
+                T v[3] = {T(0), T(0), T(0)};
+                for (int k = 0; k < nk; ++k) {
+                    const int tg = pk.target[k];
+                    const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
+                    v[q] = tadd<T>(v[q], reinterpret_cast<const T*>(pk.kick[k])[i]);
+                }
+                for (int q = 0; q < 3; ++q)
+                    if (a.comb_slot[q] >= 0) ktab[a.comb_slot[q] * Sp + i] = v[q];
+            }
+        } else if (a.kicks_smem) {
+            for (int i = tid; i < nk * Sp; i += blockDim.x) {
+                const int k = i / Sp;
+                ktab[i] = reinterpret_cast<const T*>(pk.kick[k])[i - k * Sp];
+            }
+        }
+    }
+    __syncthreads();
+
+    TrackCtx<T, VEC> cx;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) cx.cp[q] = reinterpret_cast<T*>(a.c[q]);
+    if (a.has_pk) cx.bpk.init(epk, Sp, pk.slicer.negate);
+    if (a.has_acc) cx.bac.init(eacc, Sa, acc.slicer.negate);
+    cx.ktab = ktab;
+    const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
+    cx.hx = hsx + h * Sa;
+    cx.hy = hsy + h * Sa;
+    cx.hc = hcnt + h * Sa;
+    cx.tag = htag + h * Sa;
+    cx.epoch = 0;
+    cx.shared_hist = a.n_hist < (int)(blockDim.x >> 5);
+
+    if (a.stages > 0) {
+        // ---- full tiles through a TMA ring: thread 0 keeps `stages` tiles
+        // of bulk copies in flight while the CTA computes
+        const int64_t full_tiles = a.n / TILE;
+        const int64_t mine = blockIdx.x < full_tiles
+                                 ? (full_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x
+                                 : 0;
+        int nq = 0;
+        for (int q = 0; q < 6; ++q) nq += (a.load_mask >> q) & 1;
+        const unsigned stage_bytes = (unsigned)(nq * TILE * sizeof(T));
+        auto issue = [&](int64_t k) {
+            const int st = (int)(k % a.stages);
+            const int64_t tile = blockIdx.x + k * gridDim.x;
+            fence_proxy_async_smem();
+            mbar_expect_tx(bars + st, stage_bytes);
+            for (int q = 0; q < 6; ++q)
+                if ((a.load_mask >> q) & 1)
+                    bulk_g2s(ring + ((size_t)st * 6 + q) * TILE,
+                             cx.cp[q] + tile * TILE, TILE * sizeof(T),
+                             bars + st);
+        };
+        int64_t issued = 0;
+        if (tid == 0)
+            for (; issued < mine && issued < a.stages; ++issued) issue(issued);
+        int64_t k = 0;
+        for (; k < mine; ++k) {
+            const int st = (int)(k % a.stages);
+            const unsigned parity = (unsigned)((k / a.stages) & 1);
+            if (!mbar_wait(bars + st, parity, kWaitLimit)) s_fail = 1;
+            __syncthreads();
+            if (s_fail) break;
+            Tile<T, VEC> t;
+            const T* src = ring + (size_t)st * 6 * TILE + tid * VEC;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                if ((a.load_mask >> q) & 1) {
+                    VecIO<T, VEC>::ld(src + (size_t)q * TILE, t.c[q]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
+                }
+            }
+            const int64_t i0 = (blockIdx.x + k * gridDim.x) * TILE + tid * VEC;
+            run_tile<T, VEC, SHAPE, true>(prog, pk, acc, a, cx, t, i0, true);
+            __syncthreads();                 // stage st fully read
+            if (tid == 0 && k + a.stages < mine) issue(k + a.stages), ++issued;
+        }
+        if (s_fail) {
+            // report, then wait (bounded) for this CTA's copies in flight so
+            // that none lands in shared memory after the CTA has exited
+            if (tid == 0) {
+                if (prog.status) atomicMax(prog.status, PHK_DEV_TIMEOUT);
+                for (int64_t j = k; j < issued; ++j)
+                    mbar_wait(bars + (int)(j % a.stages),
+                              (unsigned)((j / a.stages) & 1), kWaitLimit);
+            }
+            __syncthreads();
+        } else if (a.n % TILE != 0 && blockIdx.x == (int)(full_tiles % gridDim.x)) {
+            // ---- the partial last tile, plain loads
+            const int64_t i0 = full_tiles * TILE + tid * VEC;
+            const bool full = i0 + VEC <= a.n;
+            Tile<T, VEC> t;
+            load_tile_plain<T, VEC>(a, cx, t, i0, full);
+            run_tile<T, VEC, SHAPE, false>(prog, pk, acc, a, cx, t, i0, full);
+        }
+    } else {
+        // ---- plain loads; every warp runs whole tiles (lanes past the end
+        // carry dead particles) so the warp-level accumulation sees 32 lanes
+        const int64_t n_tiles_grid = (a.n_tiles + gridDim.x - 1) / gridDim.x;
+        for (int64_t it = 0; it < n_tiles_grid; ++it) {
+            const int64_t tile = blockIdx.x + it * gridDim.x;
+            const int64_t i0 = (tile * blockDim.x + tid) * VEC;
+            const bool full = i0 + VEC <= a.n;
+            Tile<T, VEC> t;
+            load_tile_plain<T, VEC>(a, cx, t, i0, full);
+            run_tile<T, VEC, SHAPE, false>(prog, pk, acc, a, cx, t, i0, full);
+        }
+    }
+
+    if (a.has_acc) {
+        __syncthreads();
+        // fold the per-warp copies into copy 0, in the storage precision
+        // (fixed order; no FP64 arithmetic in the FP32 form)
+        for (int s = tid; s < Sa; s += blockDim.x) {
+            int c = hcnt[s];
+            for (int k = 1; k < a.n_hist; ++k) {
+                c += hcnt[k * Sa + s];
+                Hist<T>::merge(hsx + s, hsx + k * Sa + s);
+                Hist<T>::merge(hsy + s, hsy + k * Sa + s);
+            }
+            hcnt[s] = c;
+        }
+        int column = blockIdx.x;
+        if (a.cluster > 1) {
+            // fold the CTAs of the thread-block cluster into its rank 0
+            // through distributed shared memory
+            namespace cg = cooperative_groups;
+            cg::cluster_group cl = cg::this_cluster();
+            cl.sync();
+            const unsigned rank = cl.block_rank();
+            if (rank == 0) {
+                for (int s = tid; s < Sa; s += blockDim.x) {
+                    int c = hcnt[s];
+                    for (unsigned r = 1; r < cl.num_blocks(); ++r) {
+                        c += *cl.map_shared_rank(hcnt + s, r);
+                        Hist<T>::merge(hsx + s, cl.map_shared_rank(hsx + s, r));
+                        Hist<T>::merge(hsy + s, cl.map_shared_rank(hsy + s, r));
+                    }
+                    hcnt[s] = c;
+                }
+            }
+            cl.sync();  // members keep their shared memory until read
+            if (rank != 0) return;
+            column = blockIdx.x / a.cluster;
+        } else {
+            __syncthreads();
+        }
+        const int G = acc.grid;
+        double* P = acc.partials;
+        for (int s = tid; s < Sa; s += blockDim.x) {
+            P[(int64_t)s * G + column] = (double)hcnt[s];
+            P[(int64_t)(Sa + s) * G + column] = Hist<T>::value(hsx + s);
+            P[(int64_t)(2 * Sa + s) * G + column] = Hist<T>::value(hsy + s);
+        }
+    }
+}
+
+// ===================================================================
+// launch configuration
+// ===================================================================
+
+// Shared-memory plan of a launch: histogram copies (one private copy per
+// warp when they fit, else fewer copies shared with atomics) and TMA ring
+// stages (FP32 aligned launches), chosen so that two CTAs fit on an SM
+// whenever possible.
+template <typename T>
+static size_t smem_for(int Sa, int Sp, int nk, bool tma, int* n_hist,
+                       int* kicks_smem, int* stages) {
+    const int warps = kTrackThreads / 32;
+    const int tile = kTrackThreads * (sizeof(T) == 8 ? 2 : kF32Vec);
+    const size_t budget = sizeof(T) == 8 ? kF64SmemBudget : kF32SmemBudget;
+    *kicks_smem = (size_t)nk * Sp * sizeof(T) <= 48 * 1024;
+    const int hist_opts[4] = {warps, 4, 2, 1};
+    const int stage_opts[2] = {3, 2};
+    size_t off[9];
+    size_t best = 0;
+    for (int hi = 0; hi < 4; ++hi) {
+        for (int si = 0; si < (tma ? 2 : 1); ++si) {
+            const int nh = Sa > 0 ? hist_opts[hi] : 1;
+            const int st = tma ? stage_opts[si] : 0;
+            const size_t b = track_smem_layout<T>(Sa, Sp, nh, nk, *kicks_smem,
+                                                  st, tile, off);
+            if (best == 0 || b <= budget) {
+                *n_hist = nh;
+                *stages = st;
+                best = b;
+            }
+            if (b <= budget) return b;
+        }
+    }
+    return best;
+}
+
+// Opt the track kernel into the device's full dynamic shared memory, once
+// per instantiation and device (never inside a stream capture's hot path).
+template <typename T, int VEC, int SHAPE>
+static void prepare_track_kernel() {
+    static int done_for[64] = {0};
+    const DeviceInfo& d = device_info();
+    const int dev = d.device < 64 ? d.device : 63;
+    if (done_for[dev]) return;
+    // dynamic + static shared memory must stay within the opt-in limit
+    cudaFuncAttributes fa;
+    size_t static_smem = 0;
+    if (cudaFuncGetAttributes(&fa, track_kernel<T, VEC, SHAPE>) == cudaSuccess)
+        static_smem = fa.sharedSizeBytes;
+    else
+        cudaGetLastError();
+    if (cudaFuncSetAttribute(track_kernel<T, VEC, SHAPE>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             d.max_smem_optin - (int)static_smem) != cudaSuccess)
+        cudaGetLastError();
+    done_for[dev] = 1;
+}
+
+// largest dynamic shared memory a track launch may request
+template <typename T, int VEC, int SHAPE>
+static size_t track_dynamic_smem_limit() {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, track_kernel<T, VEC, SHAPE>) != cudaSuccess) {
+        cudaGetLastError();
+        return (size_t)device_info().max_smem_optin - 1024;
+    }
+    return (size_t)device_info().max_smem_optin - fa.sharedSizeBytes;
+}
+
+// CTAs per thread-block cluster of an accumulating launch
+constexpr int kCluster = 4;
+
+template <typename T, int VEC, int SHAPE>
+static int occupancy_blocks(size_t smem) {
+    int b = 0;
+    prepare_track_kernel<T, VEC, SHAPE>();
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &b, track_kernel<T, VEC, SHAPE>, kTrackThreads, smem) != cudaSuccess)
+        b = 1;
+    return b < 1 ? 1 : b;
+}
+
+// clusters of kCluster CTAs that can be resident at once
+template <typename T, int VEC, int SHAPE>
+static int occupancy_clusters(size_t smem) {
+    prepare_track_kernel<T, VEC, SHAPE>();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kCluster * device_info().sm_count, 1, 1);
+    cfg.blockDim = dim3(kTrackThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = kCluster;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, track_kernel<T, VEC, SHAPE>, &cfg) !=
+            cudaSuccess || n < 1) {
+        cudaGetLastError();
+        n = device_info().sm_count / kCluster;
+    }
+    return n < 1 ? 1 : n;
+}
+
+template <typename T, int VEC, int SHAPE>
+static int launch_track_t(const phk_program* prog, const phk_coords* c,
+                          const phk_kick_set* pk, const phk_accum* acc,
+                          int load_mask, int store_mask, cudaStream_t st) {
+    TrackArgs a;
+    a.c[0] = c->x; a.c[1] = c->xp; a.c[2] = c->y;
+    a.c[3] = c->yp; a.c[4] = c->z; a.c[5] = c->dp;
+    a.n = c->n;
+    a.has_pk = pk != nullptr;
+    a.has_acc = acc != nullptr;
+    a.load_mask = load_mask;
+    a.store_mask = store_mask;
+    a.cluster = 1;
+    a.stages = 0;
+    a.kick_comb = 0;
+    a.comb_slot[0] = a.comb_slot[1] = a.comb_slot[2] = -1;
+    const int64_t per_tile = (int64_t)kTrackThreads * VEC;
+    a.n_tiles = (c->n + per_tile - 1) / per_tile;
+    static phk_kick_set zero_pk;
+    static phk_accum zero_acc;
+    const int Sa = acc ? acc->slicer.n_slices : 0;
+    const int Sp = pk ? pk->slicer.n_slices : 0;
+    const int nk = pk ? pk->n_kicks : 0;
+    // the TMA ring needs 16-byte aligned coordinates (VEC > 1 launches)
+    // and pays off for the memory-bound FP32 form
+    const bool tma = VEC > 1 && sizeof(T) == 4;
+    const size_t smem = smem_for<T>(Sa, Sp, nk, tma, &a.n_hist,
+                                    &a.kicks_smem, &a.stages);
+    if (sizeof(T) == 4 && pk && a.kicks_smem) {
+        // FP32 form: dipolar kicks of one target are summed once per slice
+        // when staged (quadrupolar kicks keep the per-kick loop)
+        bool dip = true;
+        for (int k = 0; k < nk; ++k) dip = dip && pk->quad[k] < 0;
+        if (dip) {
+            a.kick_comb = 1;
+            int n = 0;
+            for (int k = 0; k < nk; ++k) {
+                const int tg = pk->target[k];
+                const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
+                if (a.comb_slot[q] < 0) a.comb_slot[q] = n++;
+            }
+        }
+    }
+    if (smem > track_dynamic_smem_limit<T, VEC, SHAPE>())
+        return set_error(PHK_ESIZE, "phk_track: %zu bytes of shared memory "
+                         "needed for %d + %d slices", smem, Sa, Sp);
+    prepare_track_kernel<T, VEC, SHAPE>();
+    cudaError_t e;
+    if (acc) {
+        // one partial column per cluster of kCluster CTAs
+        a.cluster = kCluster;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)acc->grid * kCluster, 1, 1);
+        cfg.blockDim = dim3(kTrackThreads, 1, 1);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = kCluster;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, track_kernel<T, VEC, SHAPE>, *prog, pk ? *pk : zero_pk,
+                               *acc, a);
+    } else {
+        const int bps = occupancy_blocks<T, VEC, SHAPE>(smem);
+        int64_t g = (int64_t)device_info().sm_count * bps;
+        if (a.n_tiles < g) g = a.n_tiles;
+        const int grid = (int)(g < 1 ? 1 : g);
+        track_kernel<T, VEC, SHAPE><<<grid, kTrackThreads, smem, st>>>(
+            *prog, pk ? *pk : zero_pk, zero_acc, a);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_track launch: %s", cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+static inline int op_mask(const phk_program* prog, int* load, int* store) {
+    // which coordinates the program reads / writes
+    int ld = 0, stm = 0;
+    for (int o = 0; o < prog->n_ops; ++o) {
+        const phk_op& op = prog->op[o];
+        const bool disp = op.flags & PHK_FLAG_DISPERSION;
+        switch (op.kind) {
+            case PHK_OP_TRANSVERSE:
+                ld |= 0x0F | 0x20;  // x xp y yp dp
+                stm |= 0x0F;
+                break;
+            case PHK_OP_DRIFT:
+                ld |= 0x30; stm |= 0x10;
+                break;
+            case PHK_OP_RF_KICK:
+            case PHK_OP_LINEAR_LONG:
+                ld |= 0x30; stm |= (op.kind == PHK_OP_RF_KICK ? 0x20 : 0x30);
+                if (disp) { ld |= 0x05; stm |= 0x05; }
+                break;
+            case PHK_OP_SCALE_TRANS:
+                ld |= 0x0F; stm |= 0x0F;
+                break;
+        }
+    }
+    *load = ld; *store = stm;
+    return 0;
+}
+
+// ===================================================================
+// batched form: many bunches, one persistent launch
+// ===================================================================
+
+struct BatchArgs {
+    TrackArgs a;             // coordinates, masks, has_pk / has_acc, n_hist
+    const phk_unit* units;
+    const int32_t* cta_first;
+    const phk_program* programs;
+    const void* kicks;
+    int32_t* status;
+    int32_t n_bunches;
+    int32_t n_units;
+    int32_t n_columns;
+};
+
+constexpr size_t kProgSmem = (sizeof(phk_program) + 15) & ~(size_t)15;
+
+// Per CTA: its units in order.  When the bunch changes, the CTA's per-slice
+// sums of the previous bunch go to that bunch's partial column, and the new
+// bunch's program and kick tables are staged in shared memory.
+template <typename T, int VEC, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+batch_track_kernel(const __grid_constant__ phk_kick_set pk,
+                   const __grid_constant__ phk_accum acc, const BatchArgs b) {
+    using W = typename Hist<T>::Word;
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int TILE = THREADS * VEC;
+    const TrackArgs& a = b.a;
+    const int Sa = a.has_acc ? acc.slicer.n_slices : 0;
+    const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
+    const int nk = a.has_pk ? pk.n_kicks : 0;
+    phk_program* sprog = reinterpret_cast<phk_program*>(smem);
+    unsigned char* rest = smem + kProgSmem;
+    size_t off[9];
+    track_smem_layout<T>(Sa, Sp, a.n_hist, nk, 1, 0, TILE, off);
+    W* hsx = reinterpret_cast<W*>(rest + off[0]);
+    W* hsy = reinterpret_cast<W*>(rest + off[1]);
+    int* hcnt = reinterpret_cast<int*>(rest + off[2]);
+    T* eacc = reinterpret_cast<T*>(rest + off[3]);
+    T* epk = reinterpret_cast<T*>(rest + off[4]);
+    T* ktab = reinterpret_cast<T*>(rest + off[5]);
+    int* htag = reinterpret_cast<int*>(rest + off[6]);
+    const int tid = threadIdx.x;
+
+    if (a.has_acc) {
+        const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
+        for (int i = tid; i <= Sa; i += THREADS) stage_edge<T>(eacc, i, e[i]);
+        for (int i = tid; i < a.n_hist * Sa; i += THREADS) {
+            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
+            hcnt[i] = 0; htag[i] = 0;
+        }
+    }
+    if (a.has_pk) {
+        const T* e = reinterpret_cast<const T*>(pk.slicer.edges);
+        for (int i = tid; i <= Sp; i += THREADS) stage_edge<T>(epk, i, e[i]);
+    }
+
+    TrackCtx<T, VEC> cx;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) cx.cp[q] = reinterpret_cast<T*>(a.c[q]);
+    cx.ktab = ktab;
+    const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
+    cx.hx = hsx + h * Sa;
+    cx.hy = hsy + h * Sa;
+    cx.hc = hcnt + h * Sa;
+    cx.tag = htag + h * Sa;
+    cx.epoch = 0;
+    cx.shared_hist = a.n_hist < THREADS / 32;
+    __syncthreads();
+    if (a.has_pk) cx.bpk.init(epk, Sp, pk.slicer.negate);
+    if (a.has_acc) cx.bac.init(eacc, Sa, acc.slicer.negate);
+
+    int u0 = b.cta_first[blockIdx.x], u1 = b.cta_first[blockIdx.x + 1];
+    if (u0 < 0 || u1 > b.n_units || u0 > u1) {
+        if (tid == 0 && b.status) atomicMax(b.status, PHK_DEV_BAD_TABLE);
+        u0 = u1 = 0;
+    }
+    int cur = -1, col = -1;
+    // write the CTA's sums of the current bunch to its column, then zero
+    auto flush = [&]() {
+        __syncthreads();
+        for (int s = tid; s < Sa; s += THREADS) {
+            int c = hcnt[s];
+            for (int k = 1; k < a.n_hist; ++k) {
+                c += hcnt[k * Sa + s];
+                Hist<T>::merge(hsx + s, hsx + k * Sa + s);
+                Hist<T>::merge(hsy + s, hsy + k * Sa + s);
+            }
+            const int G = b.n_columns;
+            double* P = acc.partials;
+            P[(int64_t)s * G + col] = (double)c;
+            P[(int64_t)(Sa + s) * G + col] = Hist<T>::value(hsx + s);
+            P[(int64_t)(2 * Sa + s) * G + col] = Hist<T>::value(hsy + s);
+        }
+        __syncthreads();
+        for (int i = tid; i < a.n_hist * Sa; i += THREADS) {
+            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
+            hcnt[i] = 0; htag[i] = 0;
+        }
+    };
+    for (int u = u0; u < u1; ++u) {
+        const phk_unit U = b.units[u];
+        const bool ok = U.bunch >= 0 && U.bunch < b.n_bunches &&
+                        U.start >= 0 && U.start <= U.end && U.end <= a.n &&
+                        (U.start & 3) == 0 &&
+                        (!a.has_acc || (U.column >= 0 && U.column < b.n_columns));
+        if (!ok) {
+            if (tid == 0 && b.status) atomicMax(b.status, PHK_DEV_BAD_TABLE);
+            continue;
+        }
+        if (U.bunch != cur) {
+            if (cur >= 0 && a.has_acc) flush();
+            __syncthreads();       // the previous bunch's program is done
+            const int4* src = reinterpret_cast<const int4*>(b.programs + U.bunch);
+            int4* dst = reinterpret_cast<int4*>(sprog);
+            for (int i = tid; i < (int)(sizeof(phk_program) / 16); i += THREADS)
+                dst[i] = src[i];
+            if (a.has_pk) {
+                const T* kt = reinterpret_cast<const T*>(b.kicks) +
+                              (int64_t)U.bunch * nk * Sp;
+                for (int i = tid; i < nk * Sp; i += THREADS) ktab[i] = kt[i];
+            }
+            __syncthreads();
+            cur = U.bunch;
+            col = U.column;
+        }
+        TrackArgs ua = a;
+        ua.n = U.end;
+        for (int64_t base = U.start; base < U.end; base += TILE) {
+            const int64_t i0 = base + (int64_t)tid * VEC;
+            const bool full = i0 + VEC <= U.end;
+            Tile<T, VEC> t;
+            load_tile_plain<T, VEC>(ua, cx, t, i0, full);
+            run_tile<T, VEC, SHAPE_GENERIC, false>(*sprog, pk, acc, ua, cx, t, i0,
+                                                   full);
+        }
+    }
+    if (cur >= 0 && a.has_acc) flush();
+}
+
+static_assert(sizeof(phk_program) % 16 == 0, "program copied as int4");
+
+template <typename T>
+static size_t batch_smem(int Sa, int Sp, int nk, int threads, int* n_hist) {
+    const int tile = threads * (sizeof(T) == 8 ? 2 : 4);
+    size_t off[9];
+    const int warps = threads / 32;
+    // one private histogram copy per warp when it stays within 48 KB
+    int nh = Sa > 0 ? warps : 1;
+    size_t bytes = track_smem_layout<T>(Sa, Sp, nh, nk, 1, 0, tile, off);
+    if (bytes > 48 * 1024 && Sa > 0) {
+        nh = 1;
+        bytes = track_smem_layout<T>(Sa, Sp, nh, nk, 1, 0, tile, off);
+    }
+    *n_hist = nh;
+    return kProgSmem + bytes;
+}
+
+template <typename T, int VEC, int THREADS>
+static int batch_occupancy(size_t smem) {
+    static int done_for[64] = {0};
+    const DeviceInfo& d = device_info();
+    const int dev = d.device < 64 ? d.device : 63;
+    if (!done_for[dev]) {
+        cudaFuncAttributes fa;
+        size_t st = 0;
+        if (cudaFuncGetAttributes(&fa, batch_track_kernel<T, VEC, THREADS>) ==
+            cudaSuccess)
+            st = fa.sharedSizeBytes;
+        else
+            cudaGetLastError();
+        if (cudaFuncSetAttribute(batch_track_kernel<T, VEC, THREADS>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 d.max_smem_optin - (int)st) != cudaSuccess)
+            cudaGetLastError();
+        done_for[dev] = 1;
+    }
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, batch_track_kernel<T, VEC, THREADS>, THREADS, smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        nb = 0;
+    }
+    return nb;
+}
+
+template <typename T, int VEC, int THREADS>
+static int launch_batch_t(const phk_batch* bt, const phk_coords* c,
+                          const phk_kick_set* pk, const phk_accum* acc,
+                          int ld, int stm, cudaStream_t st) {
+    BatchArgs b;
+    memset(&b, 0, sizeof(b));
+    TrackArgs& a = b.a;
+    a.c[0] = c->x; a.c[1] = c->xp; a.c[2] = c->y;
+    a.c[3] = c->yp; a.c[4] = c->z; a.c[5] = c->dp;
+    a.n = c->n;
+    a.has_pk = pk != nullptr;
+    a.has_acc = acc != nullptr;
+    a.load_mask = ld;
+    a.store_mask = stm;
+    a.kicks_smem = 1;
+    a.cluster = 1;
+    a.stages = 0;
+    const int Sa = acc ? acc->slicer.n_slices : 0;
+    const int Sp = pk ? pk->slicer.n_slices : 0;
+    const int nk = pk ? pk->n_kicks : 0;
+    const size_t smem = batch_smem<T>(Sa, Sp, nk, THREADS, &a.n_hist);
+    if (batch_occupancy<T, VEC, THREADS>(smem) < 1)
+        return set_error(PHK_ESIZE, "phk_track_batch: %zu bytes of shared "
+                         "memory for %d + %d slices do not fit", smem, Sa, Sp);
+    b.units = bt->units;
+    b.cta_first = bt->cta_first;
+    b.programs = bt->programs;
+    b.kicks = bt->kicks;
+    b.status = bt->status;
+    b.n_bunches = bt->n_bunches;
+    b.n_units = bt->n_units;
+    b.n_columns = bt->n_columns;
+    static phk_kick_set zero_pk;
+    static phk_accum zero_acc;
+    batch_track_kernel<T, VEC, THREADS><<<bt->grid, THREADS, smem, st>>>(
+        pk ? *pk : zero_pk, acc ? *acc : zero_acc, b);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_track_batch launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+static inline void track_masks(const phk_program* prog, const phk_kick_set* pk,
+                        const phk_accum* acc, int* ld_out, int* stm_out) {
+    int ld, stm;
+    op_mask(prog, &ld, &stm);
+    if (pk) {
+        ld |= 1 << PHK_Z;
+        for (int k = 0; k < pk->n_kicks; ++k) {
+            ld |= 1 << pk->target[k];
+            stm |= 1 << pk->target[k];
+            if (pk->quad[k] >= 0) ld |= 1 << pk->quad[k];
+        }
+    }
+    if (acc) ld |= (1 << PHK_Z) | (1 << PHK_X) | (1 << PHK_Y);
+    ld |= stm;
+    *ld_out = ld;
+    *stm_out = stm;
+}
+
+// ---- per-precision entry points (phk_track_f32.cu / phk_track_f64.cu)
+int program_shape(const phk_program* prog);
+int launch_track_f32(const phk_program* prog, const phk_coords* c,
+                     const phk_kick_set* pk, const phk_accum* acc, int ld,
+                     int stm, bool vec_ok, cudaStream_t st);
+int launch_track_f64(const phk_program* prog, const phk_coords* c,
+                     const phk_kick_set* pk, const phk_accum* acc, int ld,
+                     int stm, bool vec_ok, cudaStream_t st);
+int track_clusters_f32(size_t smem);
+int track_clusters_f64(size_t smem);
+int launch_batch_f32(const phk_batch* bt, const phk_coords* c,
+                     const phk_kick_set* pk, const phk_accum* acc, int ld,
+                     int stm, cudaStream_t st);
+int launch_batch_f64(const phk_batch* bt, const phk_coords* c,
+                     const phk_kick_set* pk, const phk_accum* acc, int ld,
+                     int stm, cudaStream_t st);
+int batch_per_sm_f32(int threads, size_t smem);
+int batch_per_sm_f64(int threads, size_t smem);
+
+}  // namespace phk
