@@ -237,6 +237,45 @@ typedef struct phk_wake_set {
     phk_wake_kick kick[PHK_MAX_KICKS];
 } phk_wake_set;
 
+/* ---- multi-turn wake on the tensor cores (FP32 form) --------------------
+ * The convolution of phk_wake (numpy path) for every kick of one WakeField
+ * as one Toeplitz GEMM with split bfloat16 products (hi*hi + hi*lo + lo*hi
+ * + lo*lo) accumulated in FP32 (see phk_wake_tc).  Kicks whose sampled
+ * tables are equal form one table group and share its K columns.
+ * Set n_slices, n_groups, group_lags (rows of each group's table) and
+ * n_kicks, then phk_wake_tc_plan() fills group_k0, k_total, m_tiles,
+ * splits and the sizes of a_hi / a_lo (uint16 elements each) and partials
+ * (float elements).  phk_wake_tc_expand() writes the bfloat16 operand
+ * a_hi / a_lo from tables[g] (double[group_lags[g]][2 S - 1], the layout
+ * of phk_wake_kick.table); repeat it whenever a table changes.  Per turn,
+ * phk_wake_tc_run() reads the moment ring (as phk_wake_set) and writes out[k]
+ * = factor[k] * convolution, in out_dtype. */
+typedef struct phk_wake_tc {
+    int32_t n_slices;
+    int32_t ring_len;
+    int32_t head;
+    int32_t n_kicks;
+    int32_t n_groups;
+    int32_t k_total;
+    int32_t m_tiles;
+    int32_t splits;
+    int32_t out_dtype;
+    int32_t reserved;
+    int32_t group_lags[PHK_MAX_KICKS];
+    int32_t group_k0[PHK_MAX_KICKS];
+    int32_t group_of[PHK_MAX_KICKS];  /* table group of each kick */
+    int32_t source[PHK_MAX_KICKS];    /* 0 count, 1 count*mean_x, 2 count*mean_y */
+    int32_t n_lags[PHK_MAX_KICKS];    /* stored turns each kick uses */
+    double factor[PHK_MAX_KICKS];
+    const double *tables[PHK_MAX_KICKS];
+    void *out[PHK_MAX_KICKS];
+    const double *moments;
+    void *a_hi;
+    void *a_lo;
+    float *partials;
+    int32_t *status;
+} phk_wake_tc;
+
 /* ---- batched form: many bunches in one persistent launch ---------------
  * No counterpart in the reference, which tracks one bunch per element
  * call.  The coordinates of all bunches are concatenated in one set of six
@@ -363,6 +402,12 @@ int phk_batch_finalize(const phk_accum *acc, int32_t n_bunches,
  * convolution is the one phk_wake would compute for sets[b]. */
 int phk_wake_batch(const phk_wake_set *sets, int32_t n_bunches,
                    int32_t n_slices, int32_t n_kicks, void *stream);
+
+/* Tensor-core wake (see phk_wake_tc): planning, operand expansion, and the
+ * per-turn convolution of every kick. */
+int phk_wake_tc_plan(phk_wake_tc *w, int64_t *a_elems, int64_t *partial_elems);
+int phk_wake_tc_expand(const phk_wake_tc *w, void *stream);
+int phk_wake_tc_run(const phk_wake_tc *w, void *stream);
 
 /* Slicing pass that allocates nothing and takes no workspace; no
  * counterpart in the reference.  Same results as phk_track(empty program,

@@ -94,6 +94,25 @@ class WakeSet(ctypes.Structure):
                 ('kick', WakeKick * PHK_MAX_KICKS)]
 
 
+class WakeTC(ctypes.Structure):
+    _fields_ = [('n_slices', ctypes.c_int32), ('ring_len', ctypes.c_int32),
+                ('head', ctypes.c_int32), ('n_kicks', ctypes.c_int32),
+                ('n_groups', ctypes.c_int32), ('k_total', ctypes.c_int32),
+                ('m_tiles', ctypes.c_int32), ('splits', ctypes.c_int32),
+                ('out_dtype', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('group_lags', ctypes.c_int32 * PHK_MAX_KICKS),
+                ('group_k0', ctypes.c_int32 * PHK_MAX_KICKS),
+                ('group_of', ctypes.c_int32 * PHK_MAX_KICKS),
+                ('source', ctypes.c_int32 * PHK_MAX_KICKS),
+                ('n_lags', ctypes.c_int32 * PHK_MAX_KICKS),
+                ('factor', ctypes.c_double * PHK_MAX_KICKS),
+                ('tables', ctypes.c_void_p * PHK_MAX_KICKS),
+                ('out', ctypes.c_void_p * PHK_MAX_KICKS),
+                ('moments', ctypes.c_void_p), ('a_hi', ctypes.c_void_p),
+                ('a_lo', ctypes.c_void_p), ('partials', ctypes.c_void_p),
+                ('status', ctypes.c_void_p)]
+
+
 class Unit(ctypes.Structure):
     _fields_ = [('start', ctypes.c_int64), ('end', ctypes.c_int64),
                 ('bunch', ctypes.c_int32), ('column', ctypes.c_int32)]
@@ -144,6 +163,11 @@ SIGNATURES = {
                            ctypes.c_void_p],
     'phk_wake_batch': [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                        ctypes.c_int32, ctypes.c_void_p],
+    'phk_wake_tc_plan': [ctypes.POINTER(WakeTC),
+                         ctypes.POINTER(ctypes.c_int64),
+                         ctypes.POINTER(ctypes.c_int64)],
+    'phk_wake_tc_expand': [ctypes.POINTER(WakeTC), ctypes.c_void_p],
+    'phk_wake_tc_run': [ctypes.POINTER(WakeTC), ctypes.c_void_p],
     'phk_slice_noalloc': [ctypes.POINTER(Slicer), ctypes.POINTER(Coords),
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p],

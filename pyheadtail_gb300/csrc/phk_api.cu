@@ -377,4 +377,77 @@ int phk_wake_batch(const phk_wake_set* sets, int32_t n_bunches,
                              (cudaStream_t)stream);
 }
 
+static int check_wake_tc(const phk_wake_tc* w, const char* who, bool planned) {
+    if (!w) return set_error(PHK_ENULL, "%s: w is NULL", who);
+    if (w->n_slices < 1 || w->n_slices > PHK_MAX_SLICES)
+        return set_error(PHK_ESIZE, "%s: n_slices %d", who, w->n_slices);
+    if (w->n_groups < 1 || w->n_groups > PHK_MAX_KICKS)
+        return set_error(PHK_ESIZE, "%s: n_groups %d", who, w->n_groups);
+    if (w->n_kicks < 1 || w->n_kicks > PHK_MAX_KICKS)
+        return set_error(PHK_ESIZE, "%s: n_kicks %d", who, w->n_kicks);
+    for (int g = 0; g < w->n_groups; ++g)
+        if (w->group_lags[g] < 1 || w->group_lags[g] > 4096)
+            return set_error(PHK_ESIZE, "%s: group %d lags %d", who, g,
+                             w->group_lags[g]);
+    if (!planned) return PHK_OK;
+    phk_wake_tc p = *w;
+    int64_t ae = 0, pe = 0;
+    int r = plan_wake_tc(&p, &ae, &pe);
+    if (r) return r;
+    if (p.k_total != w->k_total || p.m_tiles != w->m_tiles ||
+        p.splits != w->splits)
+        return set_error(PHK_EPARAM, "%s: plan fields do not match "
+                         "phk_wake_tc_plan", who);
+    for (int g = 0; g < w->n_groups; ++g)
+        if (p.group_k0[g] != w->group_k0[g])
+            return set_error(PHK_EPARAM, "%s: group_k0 does not match", who);
+    if (!w->a_hi || !w->a_lo)
+        return set_error(PHK_ENULL, "%s: a_hi / a_lo is NULL", who);
+    if ((reinterpret_cast<uintptr_t>(w->a_hi) |
+         reinterpret_cast<uintptr_t>(w->a_lo)) & 15)
+        return set_error(PHK_EALIGN, "%s: a_hi / a_lo not 16-byte aligned", who);
+    return PHK_OK;
+}
+
+int phk_wake_tc_plan(phk_wake_tc* w, int64_t* a_elems, int64_t* partial_elems) {
+    int r = check_wake_tc(w, "phk_wake_tc_plan", false);
+    if (r) return r;
+    return plan_wake_tc(w, a_elems, partial_elems);
+}
+
+int phk_wake_tc_expand(const phk_wake_tc* w, void* stream) {
+    const char* who = "phk_wake_tc_expand";
+    int r = check_wake_tc(w, who, true);
+    if (r) return r;
+    for (int g = 0; g < w->n_groups; ++g)
+        if (!w->tables[g])
+            return set_error(PHK_ENULL, "%s: table of group %d is NULL", who, g);
+    return launch_wake_tc_expand(w, (cudaStream_t)stream);
+}
+
+int phk_wake_tc_run(const phk_wake_tc* w, void* stream) {
+    const char* who = "phk_wake_tc_run";
+    int r = check_wake_tc(w, who, true);
+    if (r) return r;
+    if (!w->moments || !w->partials)
+        return set_error(PHK_ENULL, "%s: moments / partials is NULL", who);
+    if (w->ring_len < 1 || w->head < 0 || w->head >= w->ring_len)
+        return set_error(PHK_EPARAM, "%s: ring_len %d head %d", who,
+                         w->ring_len, w->head);
+    if ((r = check_dtype(w->out_dtype, who))) return r;
+    for (int k = 0; k < w->n_kicks; ++k) {
+        if (!w->out[k]) return set_error(PHK_ENULL, "%s: out %d is NULL", who, k);
+        if (w->group_of[k] < 0 || w->group_of[k] >= w->n_groups)
+            return set_error(PHK_EPARAM, "%s: kick %d group %d", who, k,
+                             w->group_of[k]);
+        if (w->source[k] < 0 || w->source[k] > 2)
+            return set_error(PHK_EPARAM, "%s: kick %d source %d", who, k,
+                             w->source[k]);
+        if (w->n_lags[k] < 0 || w->n_lags[k] > w->ring_len)
+            return set_error(PHK_EPARAM, "%s: kick %d n_lags %d", who, k,
+                             w->n_lags[k]);
+    }
+    return launch_wake_tc(w, (cudaStream_t)stream);
+}
+
 }  // extern "C"

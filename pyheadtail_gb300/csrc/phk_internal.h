@@ -38,6 +38,9 @@ int launch_moments(const phk_slicer* s, const void* z, int64_t n,
                    int32_t pass, const double* means, double* sums,
                    int32_t* counts, cudaStream_t stream);
 
+int plan_wake_tc(phk_wake_tc* w, int64_t* a_elems, int64_t* partial_elems);
+int launch_wake_tc_expand(const phk_wake_tc* w, cudaStream_t stream);
+int launch_wake_tc(const phk_wake_tc* w, cudaStream_t stream);
 int launch_track_batch(const phk_batch* b, const phk_coords* c,
                        const phk_kick_set* pk, const phk_accum* acc,
                        cudaStream_t stream);

@@ -1,0 +1,428 @@
+// Multi-turn wake convolution of the FP32 form as a Toeplitz GEMM on the
+// 5th-generation tensor cores (tcgen05), BF16x3 split products accumulated
+// in FP32 in tensor memory.
+//
+// For every kick k (wake_kicks.py:118-139, numpy path :87-116):
+//   out_k[i] = factor_k * sum_a sum_j T_g(k)[a][i - j + S - 1] * m_a[src_k][j]
+// with T_g the sampled wake of table group g (kicks whose tables are equal,
+// e.g. the x and y dipole kicks of a circular source, share one group) and
+// m_a the moment ring slot of stored turn a.  Written as D = A B^T:
+//   A[i][(g, a, j)] = T_g[a][i - j + S - 1]          (S x K, the Toeplitz
+//                                                     rows of every group)
+//   B[n][(g, a, j)] = m_a[src_k][j] if g(k) == g    (n = k: high part,
+//                                                     n = nk + k: low part)
+// Each operand is split into a high and a low bfloat16 part (x ~ hi + lo to
+// ~2^-16 relative); D_hi = A_hi B^T and D_lo = A_lo B^T hold all four
+// products hi*hi, hi*lo, lo*hi, lo*lo, summed in the epilogue.
+//
+// A depends only on the tables (fixed cuts and energy: constant over the
+// run), so it is expanded once into the canonical no-swizzle K-major layout
+// of the tensor-core operand, one 16 KB block per (128-row tile, 64-column
+// chunk), and streamed with bulk copies.  B is built per chunk in shared
+// memory from the FP64 moment ring.  The K range is split across CTAs; a
+// fixed-order FP64 reduction of the split partials applies the factors.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "phk_device.cuh"
+#include "phk_internal.h"
+
+namespace phk {
+
+constexpr int kTcM = 128;          // rows per tile (TMEM lanes)
+constexpr int kTcN = 16;           // B rows: hi and lo parts of <= 8 kicks
+constexpr int kTcK = 64;           // K per chunk (4 MMAs of K = 16)
+constexpr int kTcStages = 3;
+constexpr int kTcMaxChunks = 8;    // K chunks per CTA (B staged up front)
+constexpr int kTcThreads = 256;
+constexpr unsigned kTcTileBytes = kTcM * kTcK * 2;   // 16 KB per A part
+constexpr unsigned kTcBBytes = kTcN * kTcK * 2;      // 2 KB
+constexpr unsigned kTcWaitLimit = 1u << 22;
+
+// ------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ void tmem_alloc(unsigned* dst, unsigned ncols) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+            smem_addr(dst)),
+        "r"(ncols)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::
+                     : "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
+                     taddr),
+                 "r"(ncols)
+                 : "memory");
+}
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (bf16 in, fp32 accumulate)
+__device__ __forceinline__ void umma_bf16(unsigned d, uint64_t a, uint64_t b,
+                                          unsigned idesc, unsigned accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// arrive on the mbarrier once every MMA issued so far has completed
+__device__ __forceinline__ void umma_commit(unsigned long long* bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
+        "[%0];" ::"r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tc_fence_after_sync() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before_sync() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]),
+          "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+          "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory operand descriptor, canonical K-major layout without
+// swizzle: 8-row x 16-byte core matrices of 128 contiguous bytes; `lbo` is
+// the byte distance of core matrices adjacent along K, `sbo` along M/N.
+__device__ __forceinline__ uint64_t smem_desc(unsigned addr, unsigned lbo,
+                                              unsigned sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;   // descriptor version of this architecture
+    return d;                 // base offset 0, no swizzle
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N = 16, M = 128.
+constexpr unsigned kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                              ((unsigned)(kTcN >> 3) << 17) |
+                              ((unsigned)(kTcM >> 4) << 24);
+
+// element (r, k) of a tile of `rows` x 64 in the canonical layout (core
+// matrices ordered k-fastest: lbo = 128 B, sbo = 1024 B)
+__host__ __device__ __forceinline__ int tile_offset(int r, int k) {
+    return ((r >> 3) * 8 + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+__device__ __forceinline__ void split_bf16(double x, __nv_bfloat16* hi,
+                                           __nv_bfloat16* lo) {
+    const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
+    *hi = h;
+    *lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(h)));
+}
+
+// K index -> (group, lag, source slice); false past the groups' columns
+__device__ __forceinline__ bool decode_k(const phk_wake_tc& w, int kg, int* g,
+                                         int* a, int* j) {
+    int gg = w.n_groups - 1;
+    while (gg > 0 && kg < w.group_k0[gg]) --gg;
+    const int r = kg - w.group_k0[gg];
+    if (r < 0) return false;
+    const int aa = r / w.n_slices;
+    if (aa >= w.group_lags[gg]) return false;
+    *g = gg;
+    *a = aa;
+    *j = r - aa * w.n_slices;
+    return true;
+}
+
+// ------------------------------------------------------------ expansion
+__global__ void wake_expand_kernel(const __grid_constant__ phk_wake_tc w) {
+    const int S = w.n_slices;
+    const int n_chunks = w.k_total / kTcK;
+    const int64_t total = (int64_t)w.m_tiles * kTcM * w.k_total;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / w.k_total);
+        const int kg = (int)(e - (int64_t)i * w.k_total);
+        double v = 0.0;
+        int g, a, j;
+        if (i < S && decode_k(w, kg, &g, &a, &j))
+            v = w.tables[g][(int64_t)a * (2 * S - 1) + i - j + S - 1];
+        const int mt = i / kTcM, ch = kg / kTcK;
+        const int64_t at = ((int64_t)mt * n_chunks + ch) * (kTcM * kTcK) +
+                           tile_offset(i % kTcM, kg % kTcK);
+        __nv_bfloat16 h, l;
+        split_bf16(v, &h, &l);
+        reinterpret_cast<__nv_bfloat16*>(w.a_hi)[at] = h;
+        reinterpret_cast<__nv_bfloat16*>(w.a_lo)[at] = l;
+    }
+}
+
+// ------------------------------------------------------------ the GEMM
+// grid (m_tiles, splits); CTA (mt, sp) multiplies row tile mt over its
+// contiguous range of K chunks and writes FP32 partials[sp][k][row].
+__global__ void __launch_bounds__(kTcThreads, 1)
+wake_gemm_kernel(const __grid_constant__ phk_wake_tc w) {
+    // A stages [A_hi | A_lo], then the B tiles of every chunk (the
+    // no-swizzle operand layout needs 16-byte aligned core matrices)
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr unsigned kStage = 2 * kTcTileBytes;
+    unsigned char* bsm = smem + kTcStages * kStage;
+    unsigned long long* full = reinterpret_cast<unsigned long long*>(
+        bsm + kTcMaxChunks * kTcBBytes);
+    unsigned long long* done = full + kTcStages;
+    unsigned long long* fin = done + kTcStages;
+    unsigned* s_taddr = reinterpret_cast<unsigned*>(fin + 1);
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int mt = blockIdx.x, sp = blockIdx.y;
+    const int n_chunks = w.k_total / kTcK;
+    const int c0 = (int)((int64_t)n_chunks * sp / gridDim.y);
+    const int c1 = (int)((int64_t)n_chunks * (sp + 1) / gridDim.y);
+    const int nc = c1 - c0 < kTcMaxChunks ? c1 - c0 : kTcMaxChunks;
+    const int S = w.n_slices, nk = w.n_kicks;
+
+    if (tid == 0) {
+        s_fail = 0;
+        for (int s = 0; s < kTcStages; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(done + s, 1);
+        }
+        mbar_init(fin, 1);
+        mbar_fence_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(s_taddr, 32);   // D_hi: columns 0-15, D_lo: 16-31
+        tmem_relinquish();
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    const unsigned taddr = *s_taddr;
+
+    const __nv_bfloat16* ahi = reinterpret_cast<const __nv_bfloat16*>(w.a_hi);
+    const __nv_bfloat16* alo = reinterpret_cast<const __nv_bfloat16*>(w.a_lo);
+    auto issue = [&](int it) {
+        const int st = it % kTcStages;
+        const int64_t blk = ((int64_t)mt * n_chunks + c0 + it) * (kTcM * kTcK);
+        unsigned char* dst = smem + st * kStage;
+        fence_proxy_async_smem();
+        mbar_expect_tx(full + st, 2 * kTcTileBytes);
+        bulk_g2s(dst, ahi + blk, kTcTileBytes, full + st);
+        bulk_g2s(dst + kTcTileBytes, alo + blk, kTcTileBytes, full + st);
+    };
+    int issued = 0;
+    if (tid == 0)
+        for (; issued < nc && issued < kTcStages; ++issued) issue(issued);
+
+    // B of every chunk of this CTA, while the first A copies are in flight
+    for (int e = tid; e < nc * kTcN * kTcK; e += kTcThreads) {
+        const int c = e / (kTcN * kTcK);
+        const int r = e - c * (kTcN * kTcK);
+        const int n = r / kTcK, kk = r - n * kTcK;
+        double v = 0.0;
+        int g, a, j;
+        if (n < 2 * nk && decode_k(w, (c0 + c) * kTcK + kk, &g, &a, &j)) {
+            const int k = n < nk ? n : n - nk;
+            if (w.group_of[k] == g && a < w.n_lags[k]) {
+                const int slot =
+                    ((w.head - a) % w.ring_len + w.ring_len) % w.ring_len;
+                v = w.moments[((int64_t)slot * 3 + w.source[k]) * S + j];
+            }
+        }
+        __nv_bfloat16 h, l;
+        split_bf16(v, &h, &l);
+        reinterpret_cast<__nv_bfloat16*>(bsm + c * kTcBBytes)[tile_offset(n, kk)] =
+            n < nk ? h : l;
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+
+    // one thread issues the MMAs as the A stages land, refilling each stage
+    // once the MMAs that read it have completed
+    int it = 0;
+    if (tid == 0) {
+        for (; it < nc; ++it) {
+            const int st = it % kTcStages;
+            const unsigned par = (unsigned)((it / kTcStages) & 1);
+            if (!mbar_wait(full + st, par, kTcWaitLimit)) { s_fail = 1; break; }
+            tc_fence_after_sync();
+            const unsigned a_hi = smem_addr(smem + st * kStage);
+            const unsigned a_lo = a_hi + kTcTileBytes;
+            const unsigned b = smem_addr(bsm + it * kTcBBytes);
+#pragma unroll
+            for (int ks = 0; ks < kTcK / 16; ++ks) {
+                const unsigned acc = (it > 0 || ks > 0) ? 1u : 0u;
+                const uint64_t db = smem_desc(b + ks * 256, 128, 1024);
+                umma_bf16(taddr, smem_desc(a_hi + ks * 256, 128, 1024), db,
+                          kTcIdesc, acc);
+                umma_bf16(taddr + 16, smem_desc(a_lo + ks * 256, 128, 1024), db,
+                          kTcIdesc, acc);
+            }
+            umma_commit(done + st);
+            if (issued < nc) {
+                if (!mbar_wait(done + st, par, kTcWaitLimit)) {
+                    s_fail = 1;
+                    ++it;
+                    break;
+                }
+                issue(issued++);
+            }
+        }
+    }
+
+    // completion of every MMA issued (commit arrives once all are done),
+    // then, after a failure, of the bulk copies still in flight (bounded)
+    if (tid == 0) {
+        umma_commit(fin);
+        if (!mbar_wait(fin, 0, kTcWaitLimit)) s_fail = 1;
+        if (s_fail)
+            for (int j = it; j < issued; ++j)
+                mbar_wait(full + j % kTcStages, (unsigned)((j / kTcStages) & 1),
+                          kTcWaitLimit);
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+
+    if (!s_fail && warp < 4) {
+        // warp q reads TMEM lanes 32q..32q+31: rows of this tile
+        float dh[16], dl[16];
+        const unsigned lane_base = (unsigned)(warp * 32) << 16;
+        if (nc > 0) {
+            tmem_ld16(taddr + lane_base, dh);
+            tmem_ld16(taddr + lane_base + 16, dl);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 16; ++c) dh[c] = dl[c] = 0.f;
+        }
+        const int row = mt * kTcM + warp * 32 + (tid & 31);
+        const int rows = w.m_tiles * kTcM;
+        for (int k = 0; k < nk; ++k) {
+            // hi*hi + hi*lo + lo*hi + lo*lo
+            const float v = (dh[k] + dh[nk + k]) + (dl[k] + dl[nk + k]);
+            w.partials[((int64_t)sp * nk + k) * rows + row] = v;
+        }
+    }
+    if (s_fail && tid == 0 && w.status) atomicMax(w.status, PHK_DEV_TIMEOUT);
+    tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(taddr, 32);
+}
+
+// fixed-order FP64 sum of the split partials, times the kick factor; eight
+// independent accumulators keep eight loads in flight per thread
+__global__ void wake_tc_reduce_kernel(const __grid_constant__ phk_wake_tc w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int S = w.n_slices;
+    const int k = t / S, i = t - k * S;
+    if (k >= w.n_kicks) return;
+    const int64_t rows = (int64_t)w.m_tiles * kTcM;
+    const int64_t stride = (int64_t)w.n_kicks * rows;
+    const float* p = w.partials + k * rows + i;
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int sp = 0;
+    for (; sp + 8 <= w.splits; sp += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[u] += (double)p[(sp + u) * stride];
+    }
+    for (int u = 0; sp < w.splits; ++sp, ++u) acc[u] += (double)p[sp * stride];
+    const double s = ((acc[0] + acc[1]) + (acc[2] + acc[3])) +
+                     ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+    const double r = w.factor[k] * s;
+    if (w.out_dtype == PHK_F64)
+        reinterpret_cast<double*>(w.out[k])[i] = r;
+    else
+        reinterpret_cast<float*>(w.out[k])[i] = (float)r;
+}
+
+size_t wake_tc_smem() {
+    return kTcStages * 2 * kTcTileBytes + kTcMaxChunks * kTcBBytes +
+           (2 * kTcStages + 1) * 8 + 16;
+}
+
+// K layout, tiles and split of a GEMM (fills k_total, m_tiles, splits and
+// group_k0 of w from n_slices, n_groups and group_lags)
+int plan_wake_tc(phk_wake_tc* w, int64_t* a_elems, int64_t* partial_elems) {
+    int64_t k = 0;
+    for (int g = 0; g < w->n_groups; ++g) {
+        w->group_k0[g] = (int32_t)k;
+        k += (int64_t)w->group_lags[g] * w->n_slices;
+    }
+    k = (k + kTcK - 1) / kTcK * kTcK;
+    if (k > (int64_t)1 << 30)
+        return set_error(PHK_ESIZE, "phk_wake_tc_plan: K = %lld too large",
+                         (long long)k);
+    w->k_total = (int32_t)k;
+    w->m_tiles = (w->n_slices + kTcM - 1) / kTcM;
+    const int chunks = (int)(k / kTcK);
+    // two CTAs per SM, at most kTcMaxChunks chunks per CTA
+    int splits = 2 * device_info().sm_count / w->m_tiles;
+    if (splits > chunks / 2) splits = chunks / 2;
+    const int need = (chunks + kTcMaxChunks - 1) / kTcMaxChunks;
+    if (splits < need) splits = need;
+    if (splits < 1) splits = 1;
+    w->splits = splits;
+    if (a_elems) *a_elems = (int64_t)w->m_tiles * kTcM * k;
+    if (partial_elems)
+        *partial_elems = (int64_t)splits * w->n_kicks * w->m_tiles * kTcM;
+    return PHK_OK;
+}
+
+int launch_wake_tc_expand(const phk_wake_tc* w, cudaStream_t st) {
+    const int64_t total = (int64_t)w->m_tiles * kTcM * w->k_total;
+    int64_t blocks = (total + 255) / 256;
+    const int64_t cap = (int64_t)device_info().sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    wake_expand_kernel<<<(unsigned)blocks, 256, 0, st>>>(*w);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_wake_tc_expand launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+int launch_wake_tc(const phk_wake_tc* w, cudaStream_t st) {
+    static int attr_done[64] = {0};
+    const DeviceInfo& d = device_info();
+    const int dev = d.device < 64 ? d.device : 63;
+    const size_t smem = wake_tc_smem();
+    if (!attr_done[dev]) {
+        if (cudaFuncSetAttribute(wake_gemm_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(PHK_ECUDA, "phk_wake_tc: shared memory attribute");
+        }
+        attr_done[dev] = 1;
+    }
+    wake_gemm_kernel<<<dim3(w->m_tiles, w->splits), kTcThreads, smem, st>>>(*w);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_wake_tc launch: %s",
+                         cudaGetErrorString(e));
+    const int n = w->n_kicks * w->n_slices;
+    wake_tc_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(*w);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_wake_tc reduce launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(2);
+    return PHK_OK;
+}
+
+}  // namespace phk

@@ -11,7 +11,8 @@ its variants (:627-678), same constructors and the same
   1. ages of the stored slice sets += C / (beta c)          (wakes.py:135-137)
   2. one fused pass: pending kicks + pending program + slicing; the fixed-
      order merge writes counts, mean_x, mean_y and the moment ring slot
-  3. ``phk_wake``: every kick's multi-turn convolution on the device
+  3. ``phk_wake``: every kick's multi-turn convolution on the device (FP32
+     form: ``phk_wake_tc_run``, a BF16x3 Toeplitz GEMM on the tensor cores)
   4. the kicks are left pending on the beam (applied by the next pass).
 ``WakeTable`` (tabulated wakes) is not part of this package.
 """
@@ -45,10 +46,92 @@ class _RingState(object):
         self.kick_out = torch.zeros(max(n_kicks, 1), n_slices,
                                     dtype=E.torch_dtype(code), device=device)
         self.head = -1
+        self.tensor = None
 
     def matches(self, n_slices, code, device):
         return (self.n_slices == n_slices and self.code == code and
                 self.device == device)
+
+
+class _TensorWake(object):
+    """Tensor-core convolution (phk_wake_tc_*) of the kicks of one WakeField
+    in the FP32 form.  Kicks whose sampled tables are equal share a table
+    group; the bfloat16 operand is re-expanded whenever a table changes
+    (for fixed cuts and energy: during the first n_turns_wake turns)."""
+
+    def __init__(self, device):
+        self.device = device
+        self._sig = None
+        self.w = None
+
+    @staticmethod
+    def signature(kicks):
+        return tuple((id(k._table), tuple(
+            None if key is None else (id(key[0]), id(key[1]), key[2], key[3])
+            for key in k._keys)) for k in kicks)
+
+    def _regroup(self, kicks, n_slices):
+        reps, group_of = [], []
+        for k in kicks:
+            for g, r in enumerate(reps):
+                if r._table.shape == k._table.shape and \
+                        torch.equal(r._table, k._table):
+                    group_of.append(g)
+                    break
+            else:
+                group_of.append(len(reps))
+                reps.append(k)
+        w = N.WakeTC()
+        w.n_slices = n_slices
+        w.n_kicks = len(kicks)
+        w.n_groups = len(reps)
+        for g, r in enumerate(reps):
+            w.group_lags[g] = r.n_turns_wake
+            w.tables[g] = r._table.data_ptr()
+        for i, g in enumerate(group_of):
+            w.group_of[i] = g
+        a_el, p_el = ctypes.c_int64(), ctypes.c_int64()
+        N.call('phk_wake_tc_plan', ctypes.byref(w), ctypes.byref(a_el),
+               ctypes.byref(p_el))
+        if self.w is None or self.a_hi.numel() != a_el.value:
+            self.a_hi = torch.empty(a_el.value, dtype=torch.int16,
+                                    device=self.device)
+            self.a_lo = torch.empty(a_el.value, dtype=torch.int16,
+                                    device=self.device)
+        if self.w is None or self.partials.numel() != p_el.value:
+            self.partials = torch.empty(p_el.value, dtype=torch.float32,
+                                        device=self.device)
+        w.a_hi = self.a_hi.data_ptr()
+        w.a_lo = self.a_lo.data_ptr()
+        w.partials = self.partials.data_ptr()
+        self.w = w
+        self.reps = reps
+
+    def run(self, kicks, ws):
+        sig = self.signature(kicks)
+        if sig != self._sig:
+            self._regroup(kicks, ws.n_slices)
+            N.call('phk_wake_tc_expand', ctypes.byref(self.w),
+                   E.stream_handle())
+            self._sig = sig
+        w = self.w
+        w.ring_len, w.head = ws.ring_len, ws.head
+        w.out_dtype = ws.out_dtype
+        w.moments = ws.moments
+        for k in range(len(kicks)):
+            st = ws.kick[k]
+            w.source[k] = st.source
+            w.n_lags[k] = st.n_lags
+            w.factor[k] = st.factor
+            w.out[k] = st.out
+        N.call('phk_wake_tc_run', ctypes.byref(w), E.stream_handle())
+
+
+def _tensor_path(kicks, bunch):
+    """FP32 form with every kick on the convolution path (fixed slicing):
+    the wake runs as a tensor-core GEMM."""
+    return (bunch._code == N.PHK_F32 and 0 < len(kicks) <= N.PHK_MAX_KICKS
+            and not any(k._dense for k in kicks))
 
 
 def _run_kicks(kicks, bunch, slice_sets, ages, state=None):
@@ -71,7 +154,12 @@ def _run_kicks(kicks, bunch, slice_sets, ages, state=None):
         out = state.kick_out[k]
         kick._fill(ws.kick[k], bunch, slice_sets, ages, out)
         entries.append(kick.pending_entry(out))
-    N.call('phk_wake', ctypes.byref(ws), E.stream_handle())
+    if _tensor_path(kicks, bunch):
+        if getattr(state, 'tensor', None) is None:
+            state.tensor = _TensorWake(state.moments.device)
+        state.tensor.run(kicks, ws)
+    else:
+        N.call('phk_wake', ctypes.byref(ws), E.stream_handle())
     bunch._engine.set_kick(E.PendingKick(ss._dslicer, entries))
 
 
