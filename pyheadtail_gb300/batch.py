@@ -53,7 +53,8 @@ DEFAULT_CONFIG = {'threads': 256, 'unit_tiles': 8, 'ctas_per_sm': 0}
 
 
 def _vec(code):
-    return 2 if code == N.PHK_F64 else 4
+    """Particles per thread of the batched kernel (FP64 and FP32 forms)."""
+    return 2
 
 
 # ------------------------------------------------------------ host planning

@@ -1330,8 +1330,8 @@ constexpr size_t kProgSmem = (sizeof(phk_program) + 15) & ~(size_t)15;
 // Per CTA: its units in order.  When the bunch changes, the CTA's per-slice
 // sums of the previous bunch go to that bunch's partial column, and the new
 // bunch's program and kick tables are staged in shared memory.
-template <typename T, int VEC, int THREADS>
-__global__ void __launch_bounds__(THREADS)
+template <typename T, int VEC, int THREADS, int SHAPE>
+__global__ void __launch_bounds__(THREADS, (sizeof(T) == 4 ? 1024 : 512) / THREADS)
 batch_track_kernel(const __grid_constant__ phk_kick_set pk,
                    const __grid_constant__ phk_accum acc, const BatchArgs b) {
     using W = typename Hist<T>::Word;
@@ -1430,7 +1430,20 @@ batch_track_kernel(const __grid_constant__ phk_kick_set pk,
             if (a.has_pk) {
                 const T* kt = reinterpret_cast<const T*>(b.kicks) +
                               (int64_t)U.bunch * nk * Sp;
-                for (int i = tid; i < nk * Sp; i += THREADS) ktab[i] = kt[i];
+                if (a.kick_comb) {
+                    for (int i = tid; i < Sp; i += THREADS) {
+                        T v[3] = {T(0), T(0), T(0)};
+                        for (int k = 0; k < nk; ++k) {
+                            const int tg = pk.target[k];
+                            const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
+                            v[q] = tadd<T>(v[q], kt[k * Sp + i]);
+                        }
+                        for (int q = 0; q < 3; ++q)
+                            if (a.comb_slot[q] >= 0) ktab[a.comb_slot[q] * Sp + i] = v[q];
+                    }
+                } else {
+                    for (int i = tid; i < nk * Sp; i += THREADS) ktab[i] = kt[i];
+                }
             }
             __syncthreads();
             cur = U.bunch;
@@ -1443,8 +1456,7 @@ batch_track_kernel(const __grid_constant__ phk_kick_set pk,
             const bool full = i0 + VEC <= U.end;
             Tile<T, VEC> t;
             load_tile_plain<T, VEC>(ua, cx, t, i0, full);
-            run_tile<T, VEC, SHAPE_GENERIC, false>(*sprog, pk, acc, ua, cx, t, i0,
-                                                   full);
+            run_tile<T, VEC, SHAPE, false>(*sprog, pk, acc, ua, cx, t, i0, full);
         }
     }
     if (cur >= 0 && a.has_acc) flush();
@@ -1454,7 +1466,7 @@ static_assert(sizeof(phk_program) % 16 == 0, "program copied as int4");
 
 template <typename T>
 static size_t batch_smem(int Sa, int Sp, int nk, int threads, int* n_hist) {
-    const int tile = threads * (sizeof(T) == 8 ? 2 : 4);
+    const int tile = threads * (sizeof(T) == 8 ? 2 : kF32Vec);
     size_t off[9];
     const int warps = threads / 32;
     // one private histogram copy per warp when it stays within 48 KB
@@ -1468,7 +1480,7 @@ static size_t batch_smem(int Sa, int Sp, int nk, int threads, int* n_hist) {
     return kProgSmem + bytes;
 }
 
-template <typename T, int VEC, int THREADS>
+template <typename T, int VEC, int THREADS, int SHAPE>
 static int batch_occupancy(size_t smem) {
     static int done_for[64] = {0};
     const DeviceInfo& d = device_info();
@@ -1476,12 +1488,12 @@ static int batch_occupancy(size_t smem) {
     if (!done_for[dev]) {
         cudaFuncAttributes fa;
         size_t st = 0;
-        if (cudaFuncGetAttributes(&fa, batch_track_kernel<T, VEC, THREADS>) ==
+        if (cudaFuncGetAttributes(&fa, batch_track_kernel<T, VEC, THREADS, SHAPE>) ==
             cudaSuccess)
             st = fa.sharedSizeBytes;
         else
             cudaGetLastError();
-        if (cudaFuncSetAttribute(batch_track_kernel<T, VEC, THREADS>,
+        if (cudaFuncSetAttribute(batch_track_kernel<T, VEC, THREADS, SHAPE>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  d.max_smem_optin - (int)st) != cudaSuccess)
             cudaGetLastError();
@@ -1489,7 +1501,7 @@ static int batch_occupancy(size_t smem) {
     }
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, batch_track_kernel<T, VEC, THREADS>, THREADS, smem) !=
+            &nb, batch_track_kernel<T, VEC, THREADS, SHAPE>, THREADS, smem) !=
         cudaSuccess) {
         cudaGetLastError();
         nb = 0;
@@ -1497,7 +1509,7 @@ static int batch_occupancy(size_t smem) {
     return nb;
 }
 
-template <typename T, int VEC, int THREADS>
+template <typename T, int VEC, int THREADS, int SHAPE>
 static int launch_batch_t(const phk_batch* bt, const phk_coords* c,
                           const phk_kick_set* pk, const phk_accum* acc,
                           int ld, int stm, cudaStream_t st) {
@@ -1512,13 +1524,28 @@ static int launch_batch_t(const phk_batch* bt, const phk_coords* c,
     a.load_mask = ld;
     a.store_mask = stm;
     a.kicks_smem = 1;
+    a.comb_slot[0] = a.comb_slot[1] = a.comb_slot[2] = -1;
+    if (sizeof(T) == 4 && pk) {
+        // FP32 form, dipolar kicks only: one staged table per target
+        bool dip = true;
+        for (int k = 0; k < pk->n_kicks; ++k) dip = dip && pk->quad[k] < 0;
+        if (dip) {
+            a.kick_comb = 1;
+            int n = 0;
+            for (int k = 0; k < pk->n_kicks; ++k) {
+                const int tg = pk->target[k];
+                const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
+                if (a.comb_slot[q] < 0) a.comb_slot[q] = n++;
+            }
+        }
+    }
     a.cluster = 1;
     a.stages = 0;
     const int Sa = acc ? acc->slicer.n_slices : 0;
     const int Sp = pk ? pk->slicer.n_slices : 0;
     const int nk = pk ? pk->n_kicks : 0;
     const size_t smem = batch_smem<T>(Sa, Sp, nk, THREADS, &a.n_hist);
-    if (batch_occupancy<T, VEC, THREADS>(smem) < 1)
+    if (batch_occupancy<T, VEC, THREADS, SHAPE>(smem) < 1)
         return set_error(PHK_ESIZE, "phk_track_batch: %zu bytes of shared "
                          "memory for %d + %d slices do not fit", smem, Sa, Sp);
     b.units = bt->units;
@@ -1531,7 +1558,7 @@ static int launch_batch_t(const phk_batch* bt, const phk_coords* c,
     b.n_columns = bt->n_columns;
     static phk_kick_set zero_pk;
     static phk_accum zero_acc;
-    batch_track_kernel<T, VEC, THREADS><<<bt->grid, THREADS, smem, st>>>(
+    batch_track_kernel<T, VEC, THREADS, SHAPE><<<bt->grid, THREADS, smem, st>>>(
         pk ? *pk : zero_pk, acc ? *acc : zero_acc, b);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
