@@ -1111,24 +1111,31 @@ static size_t smem_for(int Sa, int Sp, int nk, bool tma, int* n_hist,
     const size_t budget = sizeof(T) == 8 ? kF64SmemBudget : kF32SmemBudget;
     *kicks_smem = (size_t)nk * Sp * sizeof(T) <= 48 * 1024;
     const int hist_opts[4] = {warps, 4, 2, 1};
-    const int stage_opts[2] = {3, 2};
+    // ring stages (0: plain loads, the fallback for large slice counts)
+    const int stage_opts[3] = {3, 2, 0};
     size_t off[9];
-    size_t best = 0;
+    size_t smallest = 0;
     for (int hi = 0; hi < 4; ++hi) {
-        for (int si = 0; si < (tma ? 2 : 1); ++si) {
+        for (int si = 0; si < (tma ? 3 : 1); ++si) {
             const int nh = Sa > 0 ? hist_opts[hi] : 1;
             const int st = tma ? stage_opts[si] : 0;
             const size_t b = track_smem_layout<T>(Sa, Sp, nh, nk, *kicks_smem,
                                                   st, tile, off);
-            if (best == 0 || b <= budget) {
+            if (b <= budget) {
                 *n_hist = nh;
                 *stages = st;
-                best = b;
+                return b;
             }
-            if (b <= budget) return b;
+            if (smallest == 0 || b < smallest) {
+                // nothing fits the occupancy budget yet: keep the smallest
+                // plan (fewer resident CTAs per SM)
+                *n_hist = nh;
+                *stages = st;
+                smallest = b;
+            }
         }
     }
-    return best;
+    return smallest;
 }
 
 // Opt the track kernel into the device's full dynamic shared memory, once

@@ -294,3 +294,27 @@ def test_division_by_host_constants_is_correctly_rounded(lib):
         np.testing.assert_array_equal(beam.dp.cpu().numpy(), ob.dp,
                                       err_msg='divisor set %d' % i)
         np.testing.assert_array_equal(beam.z.cpu().numpy(), ob.z)
+
+
+def test_thousand_slices_both_forms(lib):
+    """C5's slicing (1000 slices, resonator + resistive wall): the shared
+    memory plan falls back to fewer resident CTAs.  FP64 against the oracle
+    at the usual bars.  FP32 against the oracle within 2e-4 of the RMS:
+    with 20 particles per slice, a particle whose FP32 z rounds across a
+    slice edge moves a few per cent of its slice's dipole moment, and the
+    kicks of every trailing slice follow (measured 4e-5 after 8 turns)."""
+    import cases as C
+    import gpu_cases as G
+    spec = dict(beam=C.beam_params(20000, 4), n_turns=8, elements=[
+        C.smooth_transverse(chroma=[2., 2.],
+                            amplitude=[1e-11, 1e-11, -5e-12]), C.rf(),
+        C.wake(C.slicer(1000), C.resonator(),
+               C.resistive_wall(n_turns_wake=5))])
+    rec, ref = _oracle_vs_gpu(spec, 8, record_turns=(7,))
+    compare(rec, ref, '1000 slices')
+    from oracle import cases as OC
+    c0 = OC.make_beam(spec['beam']).coords()
+    b32 = G.make_beam(spec['beam'], c0, precision='fp32')
+    r32 = G.run(spec, b32, n_turns=8, record_turns=(7,))
+    for k in COORDS:
+        assert rms_err(r32['t7_' + k], ref['t7_' + k]) <= 2e-4, k
