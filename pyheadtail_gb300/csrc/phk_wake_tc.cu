@@ -323,26 +323,23 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w) {
     if (warp == 0) tmem_dealloc(taddr, 32);
 }
 
-// fixed-order FP64 sum of the split partials, times the kick factor; eight
-// independent accumulators keep eight loads in flight per thread
+// fixed-order FP64 sum of the split partials, times the kick factor: one
+// warp per (kick, slice), lanes over the splits, then a fixed shuffle tree
 __global__ void wake_tc_reduce_kernel(const __grid_constant__ phk_wake_tc w) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     const int S = w.n_slices;
-    const int k = t / S, i = t - k * S;
+    const int k = gw / S, i = gw - k * S;
     if (k >= w.n_kicks) return;
     const int64_t rows = (int64_t)w.m_tiles * kTcM;
     const int64_t stride = (int64_t)w.n_kicks * rows;
     const float* p = w.partials + k * rows + i;
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int sp = 0;
-    for (; sp + 8 <= w.splits; sp += 8) {
+    double acc = 0.0;
+    for (int sp = lane; sp < w.splits; sp += 32) acc += (double)p[sp * stride];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) acc[u] += (double)p[(sp + u) * stride];
-    }
-    for (int u = 0; sp < w.splits; ++sp, ++u) acc[u] += (double)p[sp * stride];
-    const double s = ((acc[0] + acc[1]) + (acc[2] + acc[3])) +
-                     ((acc[4] + acc[5]) + (acc[6] + acc[7]));
-    const double r = w.factor[k] * s;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane != 0) return;
+    const double r = w.factor[k] * acc;
     if (w.out_dtype == PHK_F64)
         reinterpret_cast<double*>(w.out[k])[i] = r;
     else
@@ -415,8 +412,8 @@ int launch_wake_tc(const phk_wake_tc* w, cudaStream_t st) {
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_wake_tc launch: %s",
                          cudaGetErrorString(e));
-    const int n = w->n_kicks * w->n_slices;
-    wake_tc_reduce_kernel<<<(n + 255) / 256, 256, 0, st>>>(*w);
+    const int64_t threads = (int64_t)w->n_kicks * w->n_slices * 32;
+    wake_tc_reduce_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(*w);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_wake_tc reduce launch: %s",
