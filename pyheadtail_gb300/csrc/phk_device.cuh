@@ -199,20 +199,26 @@ __device__ __forceinline__ int32_t outside_index(double z, double tail,
 
 // --------------------------------------------------- FP32 sin/cos of 2 pi f
 // sin and cos of 2*pi*f for |f| <= 1/2 turn: quadrant q = rint(4 f) and the
-// exact remainder r = f - q/4 in [-1/8, 1/8] turn, theta = 2 pi r, then the
-// Maclaurin series of sin (to theta^9) and cos (to theta^8); truncation
-// error below 2e-9 and 2.5e-8 on |theta| <= pi/4.  The quadrant rotates
-// (s, c) by q * 90 degrees.  About 20 FP32 instructions.
+// exact remainder r = f - q/4 in [-1/8, 1/8] turn, theta = 2 pi r with 2 pi
+// split into a float and its residual (so theta carries no systematic
+// scale error), then the Maclaurin series of sin (to theta^11) and cos (to
+// theta^10): truncation error below 1e-11 and 2e-10 on |theta| <= pi/4, far
+// under the FP32 rounding of the result.  A truncation error of fixed sign
+// would make cos^2 + sin^2 drift from 1 the same way every turn, growing the
+// betatron amplitude -- and, through amplitude detuning, the phase error --
+// secularly.  The quadrant rotates (s, c) by q * 90 degrees.
 __device__ __forceinline__ void sincos_2pi(float f, float* s, float* c) {
     const float q = rintf(4.0f * f);
     const float r = fmaf(-0.25f, q, f);
-    const float th = 6.28318530717958647692f * r;
+    const float th = fmaf(r, 6.28318548202514648438f, r * -1.7484556e-7f);
     const float t2 = th * th;
-    float ps = fmaf(t2, 2.7557319224e-6f, -1.9841269841e-4f);   //  1/9!, -1/7!
+    float ps = fmaf(t2, -2.5052108385e-8f, 2.7557319224e-6f);   // -1/11!, 1/9!
+    ps = fmaf(t2, ps, -1.9841269841e-4f);                        // -1/7!
     ps = fmaf(t2, ps, 8.3333333333e-3f);                         //  1/5!
     ps = fmaf(t2, ps, -1.6666666667e-1f);                        // -1/3!
     const float sn = fmaf(th * t2, ps, th);
-    float pc = fmaf(t2, 2.4801587302e-5f, -1.3888888889e-3f);    //  1/8!, -1/6!
+    float pc = fmaf(t2, -2.7557319224e-7f, 2.4801587302e-5f);    // -1/10!, 1/8!
+    pc = fmaf(t2, pc, -1.3888888889e-3f);                        // -1/6!
     pc = fmaf(t2, pc, 4.1666666667e-2f);                         //  1/4!
     pc = fmaf(t2, pc, -0.5f);                                    // -1/2!
     const float cs = fmaf(t2, pc, 1.0f);

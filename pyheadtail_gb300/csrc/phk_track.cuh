@@ -299,10 +299,14 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
             float sx, cx, sy, cy;
             sincos_turns(qxh, qxl, dqx[j], &sx, &cx);
             sincos_turns(qyh, qyl, dqy[j], &sy, &cy);
+            // I and J are float-float (p[40..55] their low parts)
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                M[e][j] = fmaf(p[e], cx, p[8 + e] * sx);
-                M[4 + e][j] = fmaf(p[4 + e], cy, p[12 + e] * sy);
+                M[e][j] = fmaf(p[e], cx, fmaf(p[8 + e], sx,
+                                              fmaf(p[40 + e], cx, p[48 + e] * sx)));
+                M[4 + e][j] = fmaf(p[4 + e], cy,
+                                   fmaf(p[12 + e], sy,
+                                        fmaf(p[44 + e], cy, p[52 + e] * sy)));
             }
         }
     } else {
@@ -311,16 +315,25 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
 #pragma unroll
             for (int e = 0; e < 8; ++e) M[e][j] = p[e];
     }
+    // low parts of a constant matrix (zero for a per-particle one)
+    const bool ml = !(op.flags & PHK_FLAG_DETUNED);
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
         if (disp) {
             x[j] = fmaf(-Dx0, dp[j], x[j]);
             y[j] = fmaf(-Dy0, dp[j], y[j]);
         }
-        const float nx = fmaf(M[0][j], x[j], M[1][j] * xp[j]);
-        const float nxp = fmaf(M[2][j], x[j], M[3][j] * xp[j]);
-        const float ny = fmaf(M[4][j], y[j], M[5][j] * yp[j]);
-        const float nyp = fmaf(M[6][j], y[j], M[7][j] * yp[j]);
+        float cxr = 0.f, cxp = 0.f, cyr = 0.f, cyp = 0.f;
+        if (ml) {
+            cxr = fmaf(p[40], x[j], p[41] * xp[j]);
+            cxp = fmaf(p[42], x[j], p[43] * xp[j]);
+            cyr = fmaf(p[44], y[j], p[45] * yp[j]);
+            cyp = fmaf(p[46], y[j], p[47] * yp[j]);
+        }
+        const float nx = fmaf(M[0][j], x[j], fmaf(M[1][j], xp[j], cxr));
+        const float nxp = fmaf(M[2][j], x[j], fmaf(M[3][j], xp[j], cxp));
+        const float ny = fmaf(M[4][j], y[j], fmaf(M[5][j], yp[j], cyr));
+        const float nyp = fmaf(M[6][j], y[j], fmaf(M[7][j], yp[j], cyp));
         x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
         if (disp) {
             x[j] = fmaf(Dx1, dp[j], x[j]);
@@ -332,14 +345,17 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
 template <int VEC>
 __device__ __forceinline__ void op_drift(const phk_op& op,
                                          Tile<float, VEC>& t) {
+    // p: beta_ratio, eta0 * L (hi, lo), beta_ratio lo
     const float* p = reinterpret_cast<const float*>(op.p);
-    const float br = p[0], etaL = p[1];
+    const float br = p[0], etaL = p[1], etaLl = p[2], brl = p[3];
     const bool shrink = op.flags & PHK_FLAG_SHRINK;
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
-        // z = beta_ratio * z - (eta0 * L) * dp
+        // z = beta_ratio * z - (eta0 * L) * dp, constants float-float
         const float z = t.c[PHK_Z][j];
-        t.c[PHK_Z][j] = fmaf(-etaL, t.c[PHK_DP][j], shrink ? br * z : z);
+        const float dp = t.c[PHK_DP][j];
+        const float zs = shrink ? fmaf(br, z, brl * z) : z;
+        t.c[PHK_Z][j] = fmaf(-etaL, dp, fmaf(-etaLl, dp, zs));
     }
 }
 
@@ -347,10 +363,12 @@ template <int VEC>
 __device__ __forceinline__ void op_rfkick(const phk_op& op,
                                           Tile<float, VEC>& t) {
     // p: h/C (hi, lo) turns per metre, (phi_offset+phi_lock)/2pi (hi, lo),
-    //    A/p0_new, p0_old/p0_new, p_inc/p0_new, -, D_x, D_y
+    //    A/p0_new, p0_old/p0_new, p_inc/p0_new, -, D_x, D_y, then the low
+    //    parts of A/p0_new and p0_old/p0_new
     const float* p = reinterpret_cast<const float*>(op.p);
     const float mh = p[0], ml = p[1], oh = p[2], ol = p[3];
     const float A = p[4], ratio = p[5], pinc = p[6], Dx = p[8], Dy = p[9];
+    const float Al = p[10], ratiol = p[11];
     const bool disp = op.flags & PHK_FLAG_DISPERSION;
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
@@ -360,7 +378,7 @@ __device__ __forceinline__ void op_rfkick(const phk_op& op,
             t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
         }
         const float s = sin_turns_of_product(t.c[PHK_Z][j], mh, ml, oh, ol);
-        dp = fmaf(A, s, fmaf(dp, ratio, -pinc));
+        dp = fmaf(A, s, fmaf(Al, s, fmaf(dp, ratio, fmaf(dp, ratiol, -pinc))));
         if (disp) {
             t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
             t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);
@@ -371,9 +389,10 @@ __device__ __forceinline__ void op_rfkick(const phk_op& op,
 template <int VEC>
 __device__ __forceinline__ void op_linear_long(const phk_op& op,
                                                Tile<float, VEC>& t) {
-    // p: cos, sin, longfac, 1/longfac, D_x, D_y
+    // p: cos (hi, lo), longfac*sin (hi, lo), D_x, D_y, sin/longfac (hi, lo)
     const float* p = reinterpret_cast<const float*>(op.p);
-    const float cs = p[0], sn = p[1], lf = p[2], ilf = p[3];
+    const float cs = p[0], csl = p[1], a = p[2], al = p[3];
+    const float b = p[6], bl = p[7];
     const float Dx = p[4], Dy = p[5];
     const bool disp = op.flags & PHK_FLAG_DISPERSION;
 #pragma unroll
@@ -385,8 +404,8 @@ __device__ __forceinline__ void op_linear_long(const phk_op& op,
             t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
         }
         const float z0 = z, dp0 = dp;
-        z = fmaf(z0, cs, -(lf * dp0) * sn);
-        dp = fmaf(dp0, cs, (z0 * ilf) * sn);
+        z = fmaf(z0, cs, fmaf(-a, dp0, fmaf(z0, csl, -al * dp0)));
+        dp = fmaf(dp0, cs, fmaf(b, z0, fmaf(dp0, csl, bl * z0)));
         if (disp) {
             t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
             t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);

@@ -65,7 +65,9 @@ class Drift(LongitudinalMap):
         eta0 = self._eta0_only(beam.gamma)
         flags = N.FLAG_SHRINK if beta_ratio != 1 else 0
         p = {0: float(beta_ratio), 1: float(eta0), 2: float(self.length)}
-        pf = {0: np.float32(beta_ratio), 1: np.float32(eta0 * self.length)}
+        eh, el = E.split_ff(eta0 * self.length)
+        bh, bl = E.split_ff(beta_ratio)
+        pf = {0: bh, 1: eh, 2: el, 3: bl}
         return E.Op(N.OP_DRIFT, flags, p, pf)
 
     @clean_slices
@@ -114,11 +116,12 @@ class Kick(LongitudinalMap):
         off -= np.floor(off)
         hh, hl = E.split_ff(turns_per_m)
         oh, ol = E.split_ff(off)
-        pf = {0: hh, 1: hl, 2: oh, 3: ol,
-              4: np.float32(amplitude / p0_new),
-              5: np.float32(p0_old / p0_new),
+        ah, al = E.split_ff(amplitude / p0_new)
+        rh, rl = E.split_ff(p0_old / p0_new)
+        pf = {0: hh, 1: hl, 2: oh, 3: ol, 4: ah, 5: rh,
               6: np.float32(self.p_increment / p0_new),
-              8: np.float32(self.D_x), 9: np.float32(self.D_y)}
+              8: np.float32(self.D_x), 9: np.float32(self.D_y),
+              10: al, 11: rl}
         return E.Op(N.OP_RF_KICK, flags, p, pf)
 
     def track(self, beam):
@@ -301,9 +304,12 @@ class LinearMap(LongitudinalOneTurnMap):
         flags = N.FLAG_DISPERSION if (self.D_x or self.D_y) else 0
         p = {0: float(cosdQ_s), 1: float(sindQ_s), 2: float(longfac),
              3: float(self.D_x), 4: float(self.D_y), 5: 1. / float(longfac)}
-        pf = {0: np.float32(cosdQ_s), 1: np.float32(sindQ_s),
-              2: np.float32(longfac), 3: np.float32(1. / longfac),
-              4: np.float32(self.D_x), 5: np.float32(self.D_y)}
+        # precision form: float-float cos, longfac*sin and sin/longfac
+        ch, cl = E.split_ff(cosdQ_s)
+        ah, al = E.split_ff(longfac * sindQ_s)
+        bh, bl = E.split_ff(sindQ_s / longfac)
+        pf = {0: ch, 1: cl, 2: ah, 3: al, 4: np.float32(self.D_x),
+              5: np.float32(self.D_y), 6: bh, 7: bl}
         return E.Op(N.OP_LINEAR_LONG, flags, p, pf)
 
     def track(self, beam):

@@ -82,15 +82,17 @@ class TransverseSegmentMap(Element):
                 cc, ss = (c_x, s_x) if a < 2 else (c_y, s_y)
                 m = I[a, b] * cc + J[a, b] * ss
                 p[i] = float(m)
-                pf[i] = np.float32(m)
+                # precision form: float-float entries, so that the FP32 map
+                # carries no systematic rounding of its matrix
+                pf[i], pf[40 + i] = E.split_ff(m)
             return E.Op(N.OP_TRANSVERSE, flags, p, pf)
         flags |= N.FLAG_DETUNED
         mask = 0
         for i, (a, b) in enumerate(self._ENTRIES):
             p[i] = float(I[a, b])
             p[8 + i] = float(J[a, b])
-            pf[i] = np.float32(I[a, b])
-            pf[8 + i] = np.float32(J[a, b])
+            pf[i], pf[40 + i] = E.split_ff(I[a, b])
+            pf[8 + i], pf[48 + i] = E.split_ff(J[a, b])
             mask |= (I[a, b] != 0) << i
             mask |= (J[a, b] != 0) << (8 + i)
         p[20], p[21], p[22] = float(self.dQ_x), float(self.dQ_y), 2. * np.pi
