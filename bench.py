@@ -11,9 +11,10 @@ A step is one turn: [TransverseSegmentMap, RFSystems, WakeField].
 
 ``value``  plain FP64 form (the drop-in), device time of the turn replayed as
            a CUDA graph, inputs resident, L2 flushed between steps.
-``e2e``    the same turn through the public API (``m.track(beam)`` for each
-           element) with the step's coordinates copied from pinned host memory
-           and the turn's result (bunch centroid) read back, wall clock.
+``e2e``    the same turn(s) through the public API, wall clock: the step's
+           coordinates copied from pinned host memory into the beam's arrays,
+           one replay of the captured turn (``TurnGraph.replay``), the bunch
+           centroid read back (``beam.mean_x()``, ``beam.mean_y()``).
 ``forms``  the FP32 precision form measured the same way.
 ``--impl reference`` times the CPU oracle (a NumPy restatement of the
 reference's turn loop, bit-identical to it on the golden fixtures) on a
@@ -310,7 +311,9 @@ def time_form(w, coords, precision, steps, warmup, flush):
     evs = beam._engine.track_events
     beam._engine.track_events = None
     track_ms = [a.elapsed_time(b) for a, b in evs]
-    # e2e: public API, inputs from pinned host memory, centroid read back
+    # e2e: public API, every step the bunch from pinned host memory into
+    # the beam's coordinate arrays, one replay of the captured turn(s),
+    # the centroid read back
     host = {k: torch.from_numpy(np.ascontiguousarray(
         v.astype(np.float64 if precision == 'fp64' else np.float32))
     ).pin_memory() for k, v in coords.items()}
@@ -321,8 +324,7 @@ def time_form(w, coords, precision, steps, warmup, flush):
         t0 = time.perf_counter()
         for k, t in host.items():
             getattr(beam, k).copy_(t, non_blocking=True)
-        for m in elements:
-            m.track(beam)
+        tg.replay(1)
         cx, cy = beam.mean_x(), beam.mean_y()
         e2e_s.append(time.perf_counter() - t0)
     return dict(graph_ms=graph_ms, turns_per_step=tpg, track_ms=track_ms,
@@ -392,7 +394,8 @@ def run_ours(a, rank, world):
                          'kernel': 'phk::track_kernel',
                          'kernel_ms': track_avg,
                          'algorithmic_bytes_per_launch': bytes_pp * w['n']},
-            'e2e': {'value': w['n'] * len(r['e2e_s']) / e2e_t,
+            'e2e': {'value': w['n'] * r['turns_per_step'] *
+                    len(r['e2e_s']) / e2e_t,
                     'unit': 'macroparticle-turns/s',
                     'h2d_bytes_per_step': r['h2d'],
                     'd2h_bytes_per_step': r['d2h']},
