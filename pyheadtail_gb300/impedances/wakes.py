@@ -128,10 +128,12 @@ class _TensorWake(object):
 
 
 def _tensor_path(kicks, bunch):
-    """FP32 form with every kick on the convolution path (fixed slicing):
-    the wake runs as a tensor-core GEMM."""
+    """FP32 form, a multi-turn wake and every kick on the convolution path:
+    the wake runs as a tensor-core GEMM.  A single-turn convolution (K = S)
+    is too small to amortise the GEMM's staging and stays on phk_wake."""
     return (bunch._code == N.PHK_F32 and 0 < len(kicks) <= N.PHK_MAX_KICKS
-            and not any(k._dense for k in kicks))
+            and not any(k._dense for k in kicks)
+            and max(k.n_turns_wake for k in kicks) > 1)
 
 
 def _run_kicks(kicks, bunch, slice_sets, ages, state=None):

@@ -104,7 +104,8 @@ def test_tensor_wake_matches_fp64_convolution(lib, S, rw_turns):
 
 
 def test_fp32_wakefield_uses_the_tensor_path(lib):
-    """A FP32 WakeField with fixed cuts launches phk_wake_tc_run, and its
+    """A FP32 WakeField with a multi-turn wake and fixed cuts launches
+    phk_wake_tc_run (single-turn wakes stay on phk_wake), and its
     kicks track the FP64 WakeField's to the tolerance above."""
     import cases as C
     import gpu_cases as G
