@@ -125,11 +125,15 @@ __host__ __device__ __forceinline__ int tile_offset(int r, int k) {
     return ((r >> 3) * 8 + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
 }
 
+// hi + lo ~ x to ~2^-16 relative; the split runs in FP32 after one
+// conversion (the two parts keep 16 of FP32's 24 bits, and GB300's FP64
+// pipe would otherwise bound the operand staging)
 __device__ __forceinline__ void split_bf16(double x, __nv_bfloat16* hi,
                                            __nv_bfloat16* lo) {
-    const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
+    const float f = (float)x;
+    const __nv_bfloat16 h = __float2bfloat16_rn(f);
     *hi = h;
-    *lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(h)));
+    *lo = __float2bfloat16_rn(f - __bfloat162float(h));
 }
 
 // K index -> (group, lag, source slice); false past the groups' columns
