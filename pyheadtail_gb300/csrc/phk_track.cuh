@@ -813,14 +813,14 @@ __device__ __forceinline__ void run_tile(const phk_program& prog,
             // kicks of that target summed at staging
 #pragma unroll
             for (int j = 0; j < VEC; ++j) {
-                const int s = sl[j];
-                if (s < 0 || (!FULL && i0 + j >= a.n)) continue;
+                const bool on = sl[j] >= 0 && (FULL || i0 + j < a.n);
+                const int s = on ? sl[j] : 0;
                 if (a.comb_slot[0] >= 0)
-                    t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], cx.ktab[a.comb_slot[0] * Sp + s]);
+                    t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], on ? cx.ktab[a.comb_slot[0] * Sp + s] : T(0));
                 if (a.comb_slot[1] >= 0)
-                    t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], cx.ktab[a.comb_slot[1] * Sp + s]);
+                    t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], on ? cx.ktab[a.comb_slot[1] * Sp + s] : T(0));
                 if (a.comb_slot[2] >= 0)
-                    t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], cx.ktab[a.comb_slot[2] * Sp + s]);
+                    t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], on ? cx.ktab[a.comb_slot[2] * Sp + s] : T(0));
             }
         } else {
 #pragma unroll
