@@ -129,6 +129,27 @@ typedef struct phk_slicer {
  *  LINEAR_LONG:  p[0] = cos(2 pi Q_s), p[1] = sin(2 pi Q_s), p[2] = longfac,
  *                p[3] = D_x, p[4] = D_y, p[5] = 1/longfac
  *  SCALE_TRANS:  p[0] = sqrt(betagamma_old / betagamma_new)
+ *
+ * With PHK_F32 coordinates the same 256 bytes hold 64 floats; hi/lo pairs
+ * are float-float values (hi + lo), fractions in turns have the integer part
+ * removed:
+ *  TRANSVERSE, not detuned: f[0..7] M hi, f[40..47] M lo
+ *  TRANSVERSE, detuned:     f[0..7] I hi, f[8..15] J hi, f[40..47] I lo,
+ *                           f[48..55] J lo, f[16..17] frac(dQ_x) hi/lo,
+ *                           f[18..19] frac(dQ_y) hi/lo
+ *  TRANSVERSE, either:      f[32..35] = D_x_s0 D_x_s1 D_y_s0 D_y_s1
+ *  DRIFT:        f[0] beta_ratio hi, f[1..2] eta0 * length hi/lo,
+ *                f[3] beta_ratio lo
+ *  RF_KICK:      f[0..1] h / circumference hi/lo (turns per metre),
+ *                f[2..3] frac((phi_offset + _phi_lock) / 2 pi) hi/lo,
+ *                f[4] |q| V / (beta c) / p0_after hi, f[5] p0_before /
+ *                p0_after hi, f[6] p_increment / p0_after, f[8..9] D_x, D_y,
+ *                f[10..11] the lo parts of f[4] and f[5]
+ *  LINEAR_LONG:  f[0..1] cos hi/lo, f[2..3] longfac * sin hi/lo, f[4..5]
+ *                D_x, D_y, f[6..7] sin / longfac hi/lo
+ *  SCALE_TRANS:  f[0]
+ * and phk_detuner.c holds 32 floats: CHROMA as above (x from f[0], y from
+ * f[8]); AMPLITUDE f[0..3] = dapp / p0, f[4..9] as above.
  */
 typedef struct phk_op {
     int32_t kind;
@@ -318,6 +339,15 @@ typedef struct phk_batch {
 /* ---------------------------------------------------------------------- */
 
 int phk_abi_version(void);
+
+/* Polls of a kernel's wait for its own bulk copies or tensor-core MMAs
+ * before it gives up, stores PHK_DEV_TIMEOUT in its status word, waits
+ * (with the default limit) for what it has in flight and returns.  polls < 0
+ * restores the default (2^22 polls, of the order of a second); 0 makes every
+ * such wait give up at once, which exercises the failure path without any
+ * fault.  Process-wide; applies to launches made after the call.  No
+ * counterpart in the reference (its kernels have no waits). */
+int phk_set_wait_limit(int64_t polls);
 
 /* Number of kernels the library has launched in this process (all
  * devices, all threads): lets a caller verify which work ran natively. */

@@ -135,6 +135,7 @@ class PhkError(RuntimeError):
 # name -> (argtypes); every entry point returns int
 SIGNATURES = {
     'phk_abi_version': [],
+    'phk_set_wait_limit': [ctypes.c_int64],
     'phk_launch_count': [],
     'phk_last_error': [ctypes.c_char_p, ctypes.c_int],
     'phk_track_grid': [ctypes.c_int64, ctypes.c_int32, ctypes.c_int32],

@@ -19,6 +19,10 @@ static std::atomic<int64_t> g_launches(0);
 
 void count_launches(int n) { g_launches.fetch_add(n); }
 
+static std::atomic<unsigned> g_wait_limit(kDefaultWaitLimit);
+
+unsigned wait_limit() { return g_wait_limit.load(); }
+
 int set_error(int code, const char* fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -164,6 +168,13 @@ using namespace phk;
 extern "C" {
 
 int phk_abi_version(void) { return PHK_ABI_VERSION; }
+
+int phk_set_wait_limit(int64_t polls) {
+    g_wait_limit.store(polls < 0 ? kDefaultWaitLimit
+                                 : (unsigned)(polls > 0xffffffffLL ? 0xffffffffLL
+                                                                  : polls));
+    return PHK_OK;
+}
 
 int64_t phk_launch_count(void) { return g_launches.load(); }
 

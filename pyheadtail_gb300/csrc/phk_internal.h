@@ -11,6 +11,12 @@ namespace phk {
 // kernels launched by the library (phk_launch_count)
 void count_launches(int n);
 
+// polls of a first-level copy or MMA wait before a kernel gives up and
+// reports PHK_DEV_TIMEOUT (phk_set_wait_limit); draining waits always use
+// the default
+constexpr unsigned kDefaultWaitLimit = 1u << 22;
+unsigned wait_limit();
+
 // thread-local error message, read back by phk_last_error()
 int set_error(int code, const char* fmt, ...);
 

@@ -624,6 +624,7 @@ struct TrackArgs {
     int32_t stages;      // TMA ring stages (0: plain loads)
     int32_t kick_comb;   // kicks staged as one summed table per target
     int32_t comb_slot[3];  // table of target xp, yp, dp (-1: none)
+    uint32_t wait_limit;   // polls of a copy wait before giving up
 };
 
 template <typename T>
@@ -1015,7 +1016,7 @@ track_kernel(const __grid_constant__ phk_program prog,
         for (; k < mine; ++k) {
             const int st = (int)(k % a.stages);
             const unsigned parity = (unsigned)((k / a.stages) & 1);
-            if (!mbar_wait(bars + st, parity, kWaitLimit)) s_fail = 1;
+            if (!mbar_wait(bars + st, parity, a.wait_limit)) s_fail = 1;
             __syncthreads();
             if (s_fail) break;
             Tile<T, VEC> t;
@@ -1243,6 +1244,7 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     a.stages = 0;
     a.kick_comb = 0;
     a.comb_slot[0] = a.comb_slot[1] = a.comb_slot[2] = -1;
+    a.wait_limit = wait_limit();
     const int64_t per_tile = (int64_t)kTrackThreads * VEC;
     a.n_tiles = (c->n + per_tile - 1) / per_tile;
     static phk_kick_set zero_pk;

@@ -178,7 +178,7 @@ __global__ void wake_expand_kernel(const __grid_constant__ phk_wake_tc w) {
 // grid (m_tiles, splits); CTA (mt, sp) multiplies row tile mt over its
 // contiguous range of K chunks and writes FP32 partials[sp][k][row].
 __global__ void __launch_bounds__(kTcThreads, 1)
-wake_gemm_kernel(const __grid_constant__ phk_wake_tc w) {
+wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
     // A stages [A_hi | A_lo], then the B tiles of every chunk (the
     // no-swizzle operand layout needs 16-byte aligned core matrices)
     extern __shared__ __align__(128) unsigned char smem[];
@@ -262,7 +262,7 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w) {
         for (; it < nc; ++it) {
             const int st = it % kTcStages;
             const unsigned par = (unsigned)((it / kTcStages) & 1);
-            if (!mbar_wait(full + st, par, kTcWaitLimit)) { s_fail = 1; break; }
+            if (!mbar_wait(full + st, par, wait_limit)) { s_fail = 1; break; }
             tc_fence_after_sync();
             const unsigned a_hi = smem_addr(smem + st * kStage);
             const unsigned a_lo = a_hi + kTcTileBytes;
@@ -278,7 +278,7 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w) {
             }
             umma_commit(done + st);
             if (issued < nc) {
-                if (!mbar_wait(done + st, par, kTcWaitLimit)) {
+                if (!mbar_wait(done + st, par, wait_limit)) {
                     s_fail = 1;
                     ++it;
                     break;
@@ -411,7 +411,8 @@ int launch_wake_tc(const phk_wake_tc* w, cudaStream_t st) {
         }
         attr_done[dev] = 1;
     }
-    wake_gemm_kernel<<<dim3(w->m_tiles, w->splits), kTcThreads, smem, st>>>(*w);
+    wake_gemm_kernel<<<dim3(w->m_tiles, w->splits), kTcThreads, smem, st>>>(
+        *w, wait_limit());
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_wake_tc launch: %s",
