@@ -81,6 +81,25 @@ def flush_l2(buf):
 SPIN_CYCLES = 400000
 
 
+def max_over_ranks(x, world):
+    """Largest x over the ranks of the default process group (x itself for
+    one rank).  Works with the NCCL (CUDA tensor) and gloo (CPU) backends."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_step, ms_per_step_max, world):
+    """Whole-job throughput of `world` replicas, each processing
+    units_per_step per step, timed by the slowest rank."""
+    return world * units_per_step / (ms_per_step_max * 1e-3)
+
+
 def bunch_coords(w):
     from pyheadtail_gb300.particles.generators import \
         gaussian_bunch_coordinates
@@ -401,23 +420,19 @@ def run_ours(a, rank, world):
                     'd2h_bytes_per_step': r['d2h']},
         }
     clocks = sampler.stop()
-    # multi-GPU: independent replicas, slowest rank defines the time
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([forms['fp64']['ms_per_step'] if 'fp64' in forms
-                          else forms['fp32']['ms_per_step']], device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    if rank != 0:
-        return
     head = forms.get('fp64') or forms['fp32']
     prec = 'fp64' if 'fp64' in forms else 'fp32'
+    # multi-GPU: independent replicas, the slowest rank defines the time
+    ms_max = max_over_ranks(head['ms_per_step'], world)
+    if rank != 0:
+        return
     out = {
         'metric': 'macroparticle-turns/s on 1 GB300: FP32/batched vs FP64 '
                   'plain; % HBM roofline',
-        'value': head['value'] * world,
+        'value': job_value(w['n'] * head['turns_per_step'], ms_max, world),
         'unit': 'macroparticle-turns/s',
         'n_gpus': world, 'steps': a.steps, 'warmup': a.warmup,
-        'ms_per_step': head['ms_per_step'],
+        'ms_per_step': ms_max,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f64' if prec == 'fp64' else 'f32',
         'data': 'synthetic: seeded 6D Gaussian bunch (reference generator '
@@ -654,22 +669,18 @@ def run_batch(a, rank, world):
             'particles': n,
         }
     clocks = sampler.stop()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([max(f['ms_per_step'] for f in forms.values())],
-                         device='cuda')
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    if rank != 0:
-        return
     prec = 'fp32' if 'fp32' in forms else 'fp64'
     head = forms[prec]
+    ms_max = max_over_ranks(head['ms_per_step'], world)
+    if rank != 0:
+        return
     out = {
         'metric': 'macroparticle-turns/s on 1 GB300: FP32/batched vs FP64 '
                   'plain; % HBM roofline',
-        'value': head['value'] * world,
+        'value': job_value(head['particles'], ms_max, world),
         'unit': 'macroparticle-turns/s',
         'n_gpus': world, 'steps': steps, 'warmup': a.warmup,
-        'ms_per_step': head['ms_per_step'],
+        'ms_per_step': ms_max,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32' if prec == 'fp32' else 'f64',
         'data': 'synthetic: 256 seeded matched Gaussian bunches drawn on the '
