@@ -336,6 +336,48 @@ typedef struct phk_batch {
     int32_t *status;            /* device word or NULL */
 } phk_batch;
 
+/* ---- bunch statistics: Particles.mean_* / sigma_* / epsn_* /
+ *      dispersion_* / *_Twiss_* (particles/particles.py:311-390) from the
+ *      moments of cobra_functions/stats.pyx:17-185, whose cov() is a
+ *      shifted single pass with the shift a[0] (stats.pyx:34-45):
+ *          cov(a, b) = (S_ab - S_a S_b / n) / (n - 1),
+ *          S_a = sum_i (a_i - a_0),  S_ab = sum_i (a_i - a_0)(b_i - b_0).
+ * One pass over the coordinates computes the sums every statistic needs,
+ * with the pending wake kicks applied to the particles in registers: the
+ * statistics of the state after the last WakeField.track while the kicks
+ * stay pending for the next phk_track.  A record is PHK_STATS_LEN doubles:
+ *   r[0]       n
+ *   r[1..6]    shift of x, xp, y, yp, z, dp: particle 0 (kicks applied)
+ *              for order 2; 0 for order 1
+ *   r[7..12]   S_q = sum_i (u_q,i - shift_q), q = x, xp, y, yp, z, dp
+ *   r[13..33]  S_ab for the 21 pairs a <= b in the order (x,x) (x,xp) ...
+ *              (x,dp) (xp,xp) ... (dp,dp); order 2 computes the 13 pairs
+ *              a statistic uses -- (x,x) (x,xp) (xp,xp), (y,y) (y,yp)
+ *              (yp,yp), (z,z) (z,dp) (dp,dp), and x, xp, y, yp with dp --
+ *              and writes 0 for the cross-plane ones (and order 1 for all)
+ * Entries of coordinates outside `mask` are 0.  The record goes to
+ * records + PHK_STATS_LEN * (c % capacity), where c is *cursor (0 when
+ * cursor is NULL); the call then increments *cursor, so a captured graph
+ * appends one record per replay (a negative counter counts from the end).
+ * Per CTA sums are merged in a fixed order: the record is reproducible bit
+ * for bit.  Calls that share partials / ticket must not run concurrently
+ * (same stream, or ordered streams).  FP64 form: FP64 sums.  FP32 form:
+ * per-thread compensated (Kahan) FP32 first sums and FP32 pair sums,
+ * merged in FP64. */
+#define PHK_STATS_LEN 34
+typedef struct phk_stats {
+    int32_t order;     /* 1: first sums only; 2: also the 21 pair sums    */
+    int32_t capacity;  /* records in `records` (>= 1)                     */
+    double *records;   /* device [capacity][PHK_STATS_LEN]                */
+    int64_t *cursor;   /* device record counter, or NULL                  */
+    double *partials;  /* device workspace [grid][PHK_STATS_LEN]          */
+    uint32_t *ticket;  /* device word; zero before the first call, and
+                          every call leaves it zero                        */
+    int32_t grid;      /* phk_bunch_stats_grid(n, dtype)                   */
+    int32_t mask;      /* coordinates to sum (bit q = PHK_X ... PHK_DP; 0:
+                          all six); sums of the others are written as 0  */
+} phk_stats;
+
 /* ---------------------------------------------------------------------- */
 
 int phk_abi_version(void);
@@ -461,6 +503,18 @@ int phk_wake_tc_run(const phk_wake_tc *w, void *stream);
 int phk_slice_noalloc(const phk_slicer *slicer, const phk_coords *coords,
                       int32_t *counts, double *mean_x, double *mean_y,
                       void *stream);
+
+/* CTAs of a phk_bunch_stats launch over n particles of dtype; sizes the
+ * partials workspace (grid * PHK_STATS_LEN doubles). */
+int phk_bunch_stats_grid(int64_t n, int32_t dtype);
+
+/* One statistics record of the bunch (see phk_stats): replaces the
+ * particle loops of np.mean and stats.pyx cov / std / emittance /
+ * dispersion / get_alpha / get_beta / get_gamma behind the Particles
+ * statistics methods.  pending (optional) is the kick set that the next
+ * phk_track would apply first.  Coordinates are only read. */
+int phk_bunch_stats(const phk_coords *coords, const phk_kick_set *pending,
+                    const phk_stats *stats, void *stream);
 
 #ifdef __cplusplus
 }

@@ -135,4 +135,6 @@ def run(spec, beam, n_turns=None, record_turns=None):
             rec['t%d_p0' % turn] = np.float64(beam.p0)
             rec['t%d_mean_x' % turn] = np.float64(beam.mean_x())
             rec['t%d_mean_y' % turn] = np.float64(beam.mean_y())
+            for st in spec.get('record_bunch_stats', ()):
+                rec['t%d_bs_%s' % (turn, st)] = np.float64(getattr(beam, st)())
     return rec

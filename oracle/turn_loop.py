@@ -97,18 +97,85 @@ class Beam(object):
     def coords(self):
         return {k: getattr(self, k).copy() for k in self.COORDS}
 
-    # bunch statistics: particles/particles.py:311-366, stats.pyx:17-122
+    # bunch statistics: particles/particles.py:311-390 over pmath's CPU
+    # table (general/pmath.py:183-189: np.mean and the stats.pyx functions)
     def mean_x(self):
         return np.mean(self.x)
+
+    def mean_xp(self):
+        return np.mean(self.xp)
 
     def mean_y(self):
         return np.mean(self.y)
 
+    def mean_yp(self):
+        return np.mean(self.yp)
+
     def mean_z(self):
         return np.mean(self.z)
 
+    def mean_dp(self):
+        return np.mean(self.dp)
+
+    def sigma_x(self):
+        return std(self.x)
+
+    def sigma_y(self):
+        return std(self.y)
+
     def sigma_z(self):
-        return np.sqrt(cov_shifted(self.z, self.z))
+        return std(self.z)
+
+    def sigma_xp(self):
+        return std(self.xp)
+
+    def sigma_yp(self):
+        return std(self.yp)
+
+    def sigma_dp(self):
+        return std(self.dp)
+
+    def effective_normalized_emittance_x(self):
+        return emittance(self.x, self.xp, None) * self.betagamma
+
+    def effective_normalized_emittance_y(self):
+        return emittance(self.y, self.yp, None) * self.betagamma
+
+    def effective_normalized_emittance_z(self):
+        return 4 * np.pi * emittance(self.z, self.dp, None) * self.p0 / e
+
+    def epsn_x(self):
+        return emittance(self.x, self.xp, self.dp) * self.betagamma
+
+    def epsn_y(self):
+        return emittance(self.y, self.yp, self.dp) * self.betagamma
+
+    def epsn_z(self):
+        return self.effective_normalized_emittance_z()
+
+    def dispersion_x(self):
+        return dispersion(self.x, self.dp)
+
+    def dispersion_y(self):
+        return dispersion(self.y, self.dp)
+
+    def alpha_Twiss_x(self):
+        return get_alpha(self.x, self.xp, self.dp)
+
+    def alpha_Twiss_y(self):
+        return get_alpha(self.y, self.yp, self.dp)
+
+    def beta_Twiss_x(self):
+        return get_beta(self.x, self.xp, self.dp)
+
+    def beta_Twiss_y(self):
+        return get_beta(self.y, self.yp, self.dp)
+
+    def gamma_Twiss_x(self):
+        return get_gamma(self.x, self.xp, self.dp)
+
+    def gamma_Twiss_y(self):
+        return get_gamma(self.y, self.yp, self.dp)
 
 
 def cov_shifted(a, b):
@@ -125,6 +192,75 @@ def cov_shifted(a, b):
     b_sum = np.add.accumulate(db)[-1]
     ab_sum = np.add.accumulate(da * db)[-1]
     return (ab_sum - a_sum * b_sum / n) / (n - 1)
+
+
+def std(u):
+    """stats.pyx:49-54."""
+    return np.sqrt(cov_shifted(u, u))
+
+
+def dispersion(u, dp):
+    """stats.pyx:57-70: <u dp> / <dp^2> (0 when <dp^2> is 0)."""
+    mean_u_dp = np.mean(np.multiply(u, dp))
+    mean_dp2 = np.mean(np.multiply(dp, dp))
+    if mean_dp2 > 0:
+        return mean_u_dp / mean_dp2
+    return 0
+
+
+def emittance(u, up, dp):
+    """stats.pyx:73-122: sqrt of the determinant of the beam matrix with
+    the dispersive parts removed (none when dp is None or constant)."""
+    cov_u2 = cov_shifted(u, u)
+    cov_up2 = cov_shifted(up, up)
+    cov_u_up = cov_shifted(up, u)
+    term_u2_dp = term_u_up_dp = term_up2_dp = 0.
+    if dp is not None:
+        cov_dp2 = cov_shifted(dp, dp)
+        if cov_dp2 != 0:
+            cov_u_dp = cov_shifted(u, dp)
+            cov_up_dp = cov_shifted(up, dp)
+            term_u2_dp = cov_u_dp * cov_u_dp / cov_dp2
+            term_u_up_dp = cov_u_dp * cov_up_dp / cov_dp2
+            term_up2_dp = cov_up_dp * cov_up_dp / cov_dp2
+    sigma11 = cov_u2 - term_u2_dp
+    sigma12 = cov_u_up - term_u_up_dp
+    sigma22 = cov_up2 - term_up2_dp
+    return np.sqrt(sigma11 * sigma22 - sigma12 * sigma12)
+
+
+def get_alpha(u, up, dp):
+    """stats.pyx:126-145."""
+    cov_u_up = cov_shifted(u, up)
+    cov_dp2, cov_u_dp, cov_up_dp = 1., 0., 0.
+    if dp is not None:
+        cov_dp2 = cov_shifted(dp, dp)
+        cov_u_dp = cov_shifted(u, dp)
+        cov_up_dp = cov_shifted(up, dp)
+    sigma12 = cov_u_up - cov_u_dp * cov_up_dp / cov_dp2
+    return -sigma12 / emittance(u, up, dp)
+
+
+def get_beta(u, up, dp):
+    """stats.pyx:148-165."""
+    cov_u2 = cov_shifted(u, u)
+    cov_u_dp, cov_dp2 = 0., 1.
+    if dp is not None:
+        cov_u_dp = cov_shifted(u, dp)
+        cov_dp2 = cov_shifted(dp, dp)
+    sigma11 = cov_u2 - cov_u_dp * cov_u_dp / cov_dp2
+    return sigma11 / emittance(u, up, dp)
+
+
+def get_gamma(u, up, dp):
+    """stats.pyx:168-185."""
+    cov_up2 = cov_shifted(up, up)
+    cov_up_dp, cov_dp2 = 0., 1.
+    if dp is not None:
+        cov_up_dp = cov_shifted(up, dp)
+        cov_dp2 = cov_shifted(dp, dp)
+    sigma22 = cov_up2 - cov_up_dp * cov_up_dp / cov_dp2
+    return sigma22 / emittance(u, up, dp)
 
 
 # --------------------------------------------------------------------------

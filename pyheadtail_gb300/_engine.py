@@ -249,18 +249,27 @@ class Engine(object):
         self._workspaces = {}
         self.launches = 0
         self.z_version = 0     # bumped whenever z may have changed
+        # bumped whenever the beam's state (coordinates with the pending
+        # program and kick applied) may have changed
+        self.version = 0
         # optional list; when set, (start, end) CUDA events are recorded
         # around every fused track launch (used to time the kernel alone)
         self.track_events = None
 
     # -- building
+    def touch(self):
+        """Record that the coordinates were changed from outside."""
+        self.version += 1
+
     def enqueue(self, op):
+        self.version += 1
         self.ops.append(op)
         n_det = sum(len(o.detuners) for o in self.ops)
         if len(self.ops) >= N.PHK_MAX_OPS or n_det > N.PHK_MAX_DETUNERS - 2:
             self.flush()
 
     def set_kick(self, kick):
+        self.version += 1
         if self.ops:
             self.flush()
         if self.kick is not None:

@@ -128,6 +128,16 @@ class Batch(ctypes.Structure):
                 ('kicks', ctypes.c_void_p), ('status', ctypes.c_void_p)]
 
 
+PHK_STATS_LEN = 34
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [('order', ctypes.c_int32), ('capacity', ctypes.c_int32),
+                ('records', ctypes.c_void_p), ('cursor', ctypes.c_void_p),
+                ('partials', ctypes.c_void_p), ('ticket', ctypes.c_void_p),
+                ('grid', ctypes.c_int32), ('mask', ctypes.c_int32)]
+
+
 class PhkError(RuntimeError):
     """A libphk entry point returned a non-zero status."""
 
@@ -172,6 +182,9 @@ SIGNATURES = {
     'phk_slice_noalloc': [ctypes.POINTER(Slicer), ctypes.POINTER(Coords),
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p],
+    'phk_bunch_stats_grid': [ctypes.c_int64, ctypes.c_int32],
+    'phk_bunch_stats': [ctypes.POINTER(Coords), ctypes.POINTER(KickSet),
+                        ctypes.POINTER(Stats), ctypes.c_void_p],
 }
 
 _lib = None

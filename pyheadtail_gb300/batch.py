@@ -581,6 +581,7 @@ class BatchedTurn(object):
             if eng.ops:
                 raise RuntimeError('bunch %d has pending element ops outside '
                                    'the batch' % b)
+            eng.touch()
             if eng.kick is getattr(self, '_left', {}).get(b):
                 eng.kick = None
             else:
@@ -592,6 +593,7 @@ class BatchedTurn(object):
         self._left = {}
         for b, bunch in enumerate(self.batch.bunches):
             bunch._engine.z_version += 1
+            bunch._engine.touch()
             if self.nk == 0:
                 continue
             entries = [kick.pending_entry(self.kicks[b, k])

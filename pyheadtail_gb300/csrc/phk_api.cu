@@ -461,4 +461,39 @@ int phk_wake_tc_run(const phk_wake_tc* w, void* stream) {
     return launch_wake_tc(w, (cudaStream_t)stream);
 }
 
+int phk_bunch_stats_grid(int64_t n, int32_t dtype) {
+    int r = check_dtype(dtype, "phk_bunch_stats_grid");
+    if (r) return r;
+    if (n < 0) return set_error(PHK_ESIZE, "phk_bunch_stats_grid: n < 0");
+    return stats_grid(n, dtype);
+}
+
+int phk_bunch_stats(const phk_coords* coords, const phk_kick_set* pending,
+                    const phk_stats* stats, void* stream) {
+    const char* who = "phk_bunch_stats";
+    int r = check_coords(coords, who);
+    if (r) return r;
+    if (pending && (r = check_kicks(pending, coords->dtype, who))) return r;
+    if (!stats) return set_error(PHK_ENULL, "%s: stats is NULL", who);
+    const phk_stats& s = *stats;
+    if (s.order != 1 && s.order != 2)
+        return set_error(PHK_EPARAM, "%s: order %d is not 1 or 2", who, s.order);
+    if (s.capacity < 1)
+        return set_error(PHK_ESIZE, "%s: capacity %d < 1", who, s.capacity);
+    if (s.grid < 1) return set_error(PHK_ESIZE, "%s: grid %d < 1", who, s.grid);
+    if (s.mask < 0 || s.mask > 0x3f)
+        return set_error(PHK_EPARAM, "%s: mask 0x%x has bits beyond dp", who,
+                         s.mask);
+    if (!s.records || !s.partials || !s.ticket)
+        return set_error(PHK_ENULL, "%s: records / partials / ticket is NULL",
+                         who);
+    if (reinterpret_cast<uintptr_t>(s.records) % 8 ||
+        reinterpret_cast<uintptr_t>(s.partials) % 8 ||
+        reinterpret_cast<uintptr_t>(s.cursor) % 8 ||
+        reinterpret_cast<uintptr_t>(s.ticket) % 4)
+        return set_error(PHK_EALIGN, "%s: a workspace pointer is misaligned",
+                         who);
+    return launch_stats(coords, pending, stats, (cudaStream_t)stream);
+}
+
 }  // extern "C"

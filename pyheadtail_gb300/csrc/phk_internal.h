@@ -58,5 +58,8 @@ int launch_batch_finalize(const phk_accum* acc, int nb, const int32_t* bcols,
                           cudaStream_t stream);
 int launch_wake_batch(const phk_wake_set* sets, int nb, int n_slices,
                       int n_kicks, cudaStream_t stream);
+int stats_grid(int64_t n, int32_t dtype);
+int launch_stats(const phk_coords* c, const phk_kick_set* pk,
+                 const phk_stats* s, cudaStream_t stream);
 
 }  // namespace phk

@@ -777,6 +777,89 @@ struct Bins<double> {
     }
 };
 
+// Stages the pending kicks' slice edges (as lookup keys) into `epk` and,
+// when a.kicks_smem, their tables into `ktab`: one table per kick, or with
+// a.kick_comb one summed table per target (slot a.comb_slot[target]).
+// Called by all threads of a CTA; a __syncthreads() must follow.
+template <typename T>
+__device__ __forceinline__ void stage_pending(const phk_kick_set& pk,
+                                              const TrackArgs& a, T* epk,
+                                              T* ktab, int tid, int nthreads) {
+    const int Sp = pk.slicer.n_slices;
+    const int nk = pk.n_kicks;
+    const T* e = reinterpret_cast<const T*>(pk.slicer.edges);
+    for (int i = tid; i <= Sp; i += nthreads) stage_edge<T>(epk, i, e[i]);
+    if (a.kick_comb) {
+        for (int i = tid; i < Sp; i += nthreads) {
+            T v[3] = {T(0), T(0), T(0)};
+            for (int k = 0; k < nk; ++k) {
+                const int tg = pk.target[k];
+                const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
+                v[q] = tadd<T>(v[q], reinterpret_cast<const T*>(pk.kick[k])[i]);
+            }
+            for (int q = 0; q < 3; ++q)
+                if (a.comb_slot[q] >= 0) ktab[a.comb_slot[q] * Sp + i] = v[q];
+        }
+    } else if (a.kicks_smem) {
+        for (int i = tid; i < nk * Sp; i += nthreads) {
+            const int k = i / Sp;
+            ktab[i] = reinterpret_cast<const T*>(pk.kick[k])[i - k * Sp];
+        }
+    }
+}
+
+// Wake kicks left pending by the previous WakeField.track, applied in
+// kick order to the VEC particles of a tile in registers
+// (DipoleWakeKickX/Y.apply, impedances/wake_kicks.py:207-260, and the
+// quadrupolar / constant kicks :185-202, :284-361).  `ktab` holds the
+// staged tables (stage_pending); particles outside the cuts or past the
+// end are left alone.
+template <typename T, int VEC, bool FULL>
+__device__ __forceinline__ void apply_pending(const phk_kick_set& pk,
+                                              const TrackArgs& a,
+                                              const Bins<T>& bpk,
+                                              const T* ktab, Tile<T, VEC>& t,
+                                              int64_t i0) {
+    const int Sp = pk.slicer.n_slices;
+    const int nk = pk.n_kicks;
+    int sl[VEC];
+    bpk.index_vec(t.c[PHK_Z], sl);
+    if (a.kick_comb) {
+        // FP32 form, dipolar kicks only: one table per target, the
+        // kicks of that target summed at staging
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const bool on = sl[j] >= 0 && (FULL || i0 + j < a.n);
+            const int s = on ? sl[j] : 0;
+            if (a.comb_slot[0] >= 0)
+                t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], on ? ktab[a.comb_slot[0] * Sp + s] : T(0));
+            if (a.comb_slot[1] >= 0)
+                t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], on ? ktab[a.comb_slot[1] * Sp + s] : T(0));
+            if (a.comb_slot[2] >= 0)
+                t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], on ? ktab[a.comb_slot[2] * Sp + s] : T(0));
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const int s = sl[j];
+            if (s < 0 || (!FULL && i0 + j >= a.n)) continue;
+            const T kx = t.c[PHK_X][j], ky = t.c[PHK_Y][j];
+            for (int k = 0; k < nk; ++k) {
+                T val = a.kicks_smem
+                            ? ktab[k * Sp + s]
+                            : __ldg(reinterpret_cast<const T*>(pk.kick[k]) + s);
+                const int qd = pk.quad[k];
+                if (qd == PHK_X) val = tmul<T>(val, kx);
+                else if (qd == PHK_Y) val = tmul<T>(val, ky);
+                const int tg = pk.target[k];
+                if (tg == PHK_XP) t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], val);
+                else if (tg == PHK_YP) t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], val);
+                else t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], val);
+            }
+        }
+    }
+}
+
 // Per-CTA state shared by the tile loops of the track kernel.
 template <typename T, int VEC>
 struct TrackCtx {
@@ -803,47 +886,8 @@ __device__ __forceinline__ void run_tile(const phk_program& prog,
                                          const TrackArgs& a,
                                          TrackCtx<T, VEC>& cx, Tile<T, VEC>& t,
                                          int64_t i0, bool full) {
-    const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
-    const int nk = a.has_pk ? pk.n_kicks : 0;
     // 1. wake kicks of the previous WakeField.track, in kick order
-    if (a.has_pk) {
-        int sl[VEC];
-        cx.bpk.index_vec(t.c[PHK_Z], sl);
-        if (a.kick_comb) {
-            // FP32 form, dipolar kicks only: one table per target, the
-            // kicks of that target summed at staging
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-                const bool on = sl[j] >= 0 && (FULL || i0 + j < a.n);
-                const int s = on ? sl[j] : 0;
-                if (a.comb_slot[0] >= 0)
-                    t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], on ? cx.ktab[a.comb_slot[0] * Sp + s] : T(0));
-                if (a.comb_slot[1] >= 0)
-                    t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], on ? cx.ktab[a.comb_slot[1] * Sp + s] : T(0));
-                if (a.comb_slot[2] >= 0)
-                    t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], on ? cx.ktab[a.comb_slot[2] * Sp + s] : T(0));
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < VEC; ++j) {
-                const int s = sl[j];
-                if (s < 0 || (!FULL && i0 + j >= a.n)) continue;
-                const T kx = t.c[PHK_X][j], ky = t.c[PHK_Y][j];
-                for (int k = 0; k < nk; ++k) {
-                    T val = a.kicks_smem
-                                ? cx.ktab[k * Sp + s]
-                                : __ldg(reinterpret_cast<const T*>(pk.kick[k]) + s);
-                    const int qd = pk.quad[k];
-                    if (qd == PHK_X) val = tmul<T>(val, kx);
-                    else if (qd == PHK_Y) val = tmul<T>(val, ky);
-                    const int tg = pk.target[k];
-                    if (tg == PHK_XP) t.c[PHK_XP][j] = tadd<T>(t.c[PHK_XP][j], val);
-                    else if (tg == PHK_YP) t.c[PHK_YP][j] = tadd<T>(t.c[PHK_YP][j], val);
-                    else t.c[PHK_DP][j] = tadd<T>(t.c[PHK_DP][j], val);
-                }
-            }
-        }
-    }
+    if (a.has_pk) apply_pending<T, VEC, FULL>(pk, a, cx.bpk, cx.ktab, t, i0);
     // 2. element program
     run_program_shape<T, VEC, SHAPE>(prog, t);
     // 3. slice accumulation
@@ -951,27 +995,7 @@ track_kernel(const __grid_constant__ phk_program prog,
             hcnt[i] = 0; htag[i] = 0;
         }
     }
-    if (a.has_pk) {
-        const T* e = reinterpret_cast<const T*>(pk.slicer.edges);
-        for (int i = tid; i <= Sp; i += blockDim.x) stage_edge<T>(epk, i, e[i]);
-        if (a.kick_comb) {
-            for (int i = tid; i < Sp; i += blockDim.x) {
-                T v[3] = {T(0), T(0), T(0)};
-                for (int k = 0; k < nk; ++k) {
-                    const int tg = pk.target[k];
-                    const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
-                    v[q] = tadd<T>(v[q], reinterpret_cast<const T*>(pk.kick[k])[i]);
-                }
-                for (int q = 0; q < 3; ++q)
-                    if (a.comb_slot[q] >= 0) ktab[a.comb_slot[q] * Sp + i] = v[q];
-            }
-        } else if (a.kicks_smem) {
-            for (int i = tid; i < nk * Sp; i += blockDim.x) {
-                const int k = i / Sp;
-                ktab[i] = reinterpret_cast<const T*>(pk.kick[k])[i - k * Sp];
-            }
-        }
-    }
+    if (a.has_pk) stage_pending<T>(pk, a, epk, ktab, tid, blockDim.x);
     __syncthreads();
 
     TrackCtx<T, VEC> cx;
@@ -1158,6 +1182,26 @@ static size_t smem_for(int Sa, int Sp, int nk, bool tma, int* n_hist,
     return smallest;
 }
 
+// FP32 form: dipolar kicks of one target are summed once per slice when
+// staged (quadrupolar kicks keep the per-kick loop); sets a->kick_comb and
+// a->comb_slot (a->kicks_smem already decided)
+template <typename T>
+static void plan_kick_comb(const phk_kick_set* pk, TrackArgs* a) {
+    a->kick_comb = 0;
+    a->comb_slot[0] = a->comb_slot[1] = a->comb_slot[2] = -1;
+    if (sizeof(T) != 4 || !pk || !a->kicks_smem) return;
+    bool dip = true;
+    for (int k = 0; k < pk->n_kicks; ++k) dip = dip && pk->quad[k] < 0;
+    if (!dip) return;
+    a->kick_comb = 1;
+    int n = 0;
+    for (int k = 0; k < pk->n_kicks; ++k) {
+        const int tg = pk->target[k];
+        const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
+        if (a->comb_slot[q] < 0) a->comb_slot[q] = n++;
+    }
+}
+
 // Opt the track kernel into the device's full dynamic shared memory, once
 // per instantiation and device (never inside a stream capture's hot path).
 template <typename T, int VEC, int SHAPE>
@@ -1257,21 +1301,7 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     const bool tma = VEC > 1 && sizeof(T) == 4;
     const size_t smem = smem_for<T>(Sa, Sp, nk, tma, &a.n_hist,
                                     &a.kicks_smem, &a.stages);
-    if (sizeof(T) == 4 && pk && a.kicks_smem) {
-        // FP32 form: dipolar kicks of one target are summed once per slice
-        // when staged (quadrupolar kicks keep the per-kick loop)
-        bool dip = true;
-        for (int k = 0; k < nk; ++k) dip = dip && pk->quad[k] < 0;
-        if (dip) {
-            a.kick_comb = 1;
-            int n = 0;
-            for (int k = 0; k < nk; ++k) {
-                const int tg = pk->target[k];
-                const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
-                if (a.comb_slot[q] < 0) a.comb_slot[q] = n++;
-            }
-        }
-    }
+    plan_kick_comb<T>(pk, &a);
     if (smem > track_dynamic_smem_limit<T, VEC, SHAPE>())
         return set_error(PHK_ESIZE, "phk_track: %zu bytes of shared memory "
                          "needed for %d + %d slices", smem, Sa, Sp);

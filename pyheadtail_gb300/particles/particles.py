@@ -15,6 +15,8 @@ not touch them directly; they append ops to the beam's pending program
 coordinate, a slice set or a statistic is needed.  Reading ``beam.x``
 therefore always returns the current state.
 """
+import ctypes
+
 import numpy as np
 import torch
 from scipy.constants import c, e
@@ -22,6 +24,7 @@ from scipy.constants import c, e
 from .. import _engine as E
 from .. import _native as N
 from ..general.element import Printing
+from . import statistics as S
 
 COORDS = ('x', 'xp', 'y', 'yp', 'z', 'dp')
 
@@ -58,6 +61,11 @@ class Particles(Printing):
         self._device = torch.device(kwargs.get('device', 'cuda'))
         self._c = {}
         self._engine = E.Engine(self)
+        self._exposed = 0          # bumped when a coordinate is handed out
+        self._stats_ws = None
+        self._stats_cache = None
+        self._stats_mask = 0
+        self._stats_order = 1
         self.macroparticlenumber = int(macroparticlenumber)
         self.particlenumber_per_mp = particlenumber_per_mp
         self.charge = charge
@@ -127,6 +135,7 @@ class Particles(Printing):
         if name not in self._c:
             raise AttributeError(name)
         self._engine.sync_for(name)
+        self._exposed += 1
         return self._c[name]
 
     def _set(self, name, value):
@@ -134,6 +143,7 @@ class Particles(Printing):
             return
         self._engine.flush()
         self._engine.z_version += 1
+        self._exposed += 1
         t = _as_tensor(value, self._dtype, self._device)
         if t.shape != (self.macroparticlenumber,):
             raise ValueError('lengths of given phase space coordinate arrays '
@@ -188,6 +198,7 @@ class Particles(Printing):
 
     def reorder(self, permutation, except_for_attrs=[]):
         self._engine.flush()
+        self._exposed += 1
         for attr in ['id'] + list(self.coords_n_momenta):
             if attr in except_for_attrs:
                 continue
@@ -208,96 +219,154 @@ class Particles(Printing):
         self._slice_sets = {}
 
     # -------------------------------------------------- statistics
-    def _mean(self, name):
-        return float(torch.mean(getattr(self, name).double()))
+    # Every statistic is derived from one phk_bunch_stats record of the
+    # current state: one read-only pass over the coordinates, with the
+    # pending wake kicks applied in registers (no kick pass is forced), and
+    # one 272-byte read back.  A record stays valid until the state
+    # changes (an element enqueues an op or a kick, a coordinate is set or
+    # handed out); the coordinates and the order asked for so far are
+    # remembered, so a loop asking the same statistics every turn costs one
+    # pass per turn.
+    def _stats_workspace(self):
+        if self._stats_ws is None:
+            grid = N.call('phk_bunch_stats_grid', self.macroparticlenumber,
+                          self._code)
+            dev = self._device
+            part = torch.empty(grid * S.RECORD_LEN, dtype=torch.float64,
+                               device=dev)
+            ticket = torch.zeros(1, dtype=torch.int32, device=dev)
+            rec = torch.empty(S.RECORD_LEN, dtype=torch.float64, device=dev)
+            self._stats_ws = (grid, part, ticket, rec)
+        return self._stats_ws
+
+    def stats_struct(self, records, capacity=1, cursor=None, order=2,
+                     mask=0x3f):
+        """phk_stats for a statistics pass of this bunch into ``records``
+        (a float64 CUDA tensor of capacity * 34 entries)."""
+        grid, part, ticket, _ = self._stats_workspace()
+        st = N.Stats()
+        st.order = order
+        st.capacity = capacity
+        st.records = records.data_ptr()
+        st.cursor = 0 if cursor is None else cursor.data_ptr()
+        st.partials = part.data_ptr()
+        st.ticket = ticket.data_ptr()
+        st.grid = grid
+        st.mask = mask
+        return st
+
+    def launch_stats(self, records, capacity=1, cursor=None, order=2,
+                     mask=0x3f):
+        """Queue one statistics pass of the current state (no sync)."""
+        eng = self._engine
+        if eng.ops:
+            eng.flush()
+        st = self.stats_struct(records, capacity, cursor, order, mask)
+        coords = eng.coords_struct()
+        ks = eng.kick.struct() if eng.kick is not None else None
+        N.call('phk_bunch_stats', ctypes.byref(coords),
+               ctypes.byref(ks) if ks is not None else None,
+               ctypes.byref(st), E.stream_handle())
+        eng.launches += 1
+
+    def _state_key(self):
+        return (self._exposed, self._engine.version)
+
+    def _stats_record(self, coords, order):
+        key = self._state_key()
+        cached = self._stats_cache
+        if cached is not None and cached[0] == key and \
+                cached[1].covers(coords, order):
+            return cached[1]
+        self._stats_mask |= S.mask_of(coords)
+        self._stats_order = max(self._stats_order, order)
+        rec = self._stats_workspace()[3]
+        self.launch_stats(rec, order=self._stats_order, mask=self._stats_mask)
+        r = S.StatsRecord(rec.cpu().numpy(), self._stats_mask,
+                          self._stats_order)
+        self._stats_cache = (key, r)
+        return r
+
+    def _statistic(self, name):
+        coords, order = S.NEEDS[name]
+        r = self._stats_record(coords, order)
+        return r.statistic(name, self.betagamma, self.p0, e)
 
     def mean_x(self, **kwargs):
-        return self._mean('x')
+        return self._statistic('mean_x')
 
     def mean_xp(self, **kwargs):
-        return self._mean('xp')
+        return self._statistic('mean_xp')
 
     def mean_y(self, **kwargs):
-        return self._mean('y')
+        return self._statistic('mean_y')
 
     def mean_yp(self, **kwargs):
-        return self._mean('yp')
+        return self._statistic('mean_yp')
 
     def mean_z(self, **kwargs):
-        return self._mean('z')
+        return self._statistic('mean_z')
 
     def mean_dp(self, **kwargs):
-        return self._mean('dp')
-
-    def _cov(self, a, b):
-        """Covariance with n-1 normalisation (cobra_functions/stats.pyx:17-45,
-        evaluated as a two-pass sum on the device)."""
-        a = getattr(self, a).double()
-        b = getattr(self, b).double()
-        n = a.numel()
-        if n < 2:
-            return 0.
-        return float(torch.sum((a - a.mean()) * (b - b.mean())) / (n - 1))
+        return self._statistic('mean_dp')
 
     def sigma_x(self, **kwargs):
-        return np.sqrt(self._cov('x', 'x'))
+        return self._statistic('sigma_x')
 
     def sigma_y(self, **kwargs):
-        return np.sqrt(self._cov('y', 'y'))
+        return self._statistic('sigma_y')
 
     def sigma_z(self, **kwargs):
-        return np.sqrt(self._cov('z', 'z'))
+        return self._statistic('sigma_z')
 
     def sigma_xp(self, **kwargs):
-        return np.sqrt(self._cov('xp', 'xp'))
+        return self._statistic('sigma_xp')
 
     def sigma_yp(self, **kwargs):
-        return np.sqrt(self._cov('yp', 'yp'))
+        return self._statistic('sigma_yp')
 
     def sigma_dp(self, **kwargs):
-        return np.sqrt(self._cov('dp', 'dp'))
-
-    def _emittance(self, u, up, dp):
-        """stats.pyx:83-122."""
-        cu2 = self._cov(u, u)
-        cup2 = self._cov(up, up)
-        cuup = self._cov(up, u)
-        t11 = t12 = t22 = 0.
-        if dp is not None:
-            cdp2 = self._cov(dp, dp)
-            if cdp2 != 0:
-                cudp = self._cov(u, dp)
-                cupdp = self._cov(up, dp)
-                t11 = cudp * cudp / cdp2
-                t12 = cudp * cupdp / cdp2
-                t22 = cupdp * cupdp / cdp2
-        s11, s12, s22 = cu2 - t11, cuup - t12, cup2 - t22
-        return np.sqrt(s11 * s22 - s12 * s12)
+        return self._statistic('sigma_dp')
 
     def effective_normalized_emittance_x(self, **kwargs):
-        return self._emittance('x', 'xp', None) * self.betagamma
+        return self._statistic('effective_normalized_emittance_x')
 
     def effective_normalized_emittance_y(self, **kwargs):
-        return self._emittance('y', 'yp', None) * self.betagamma
+        return self._statistic('effective_normalized_emittance_y')
 
     def effective_normalized_emittance_z(self, **kwargs):
-        return 4 * np.pi * self._emittance('z', 'dp', None) * self.p0 / e
+        return self._statistic('effective_normalized_emittance_z')
 
     def epsn_x(self, **kwargs):
-        return self._emittance('x', 'xp', 'dp') * self.betagamma
+        return self._statistic('epsn_x')
 
     def epsn_y(self, **kwargs):
-        return self._emittance('y', 'yp', 'dp') * self.betagamma
+        return self._statistic('epsn_y')
 
     def epsn_z(self, **kwargs):
-        return self.effective_normalized_emittance_z(**kwargs)
+        # always the effective emittance (particles.py:363-365)
+        return self._statistic('epsn_z')
 
     def dispersion_x(self):
-        x, dp = self.x.double(), self.dp.double()
-        d2 = float(torch.mean(dp * dp))
-        return float(torch.mean(x * dp)) / d2 if d2 > 0 else 0
+        return self._statistic('dispersion_x')
 
     def dispersion_y(self):
-        y, dp = self.y.double(), self.dp.double()
-        d2 = float(torch.mean(dp * dp))
-        return float(torch.mean(y * dp)) / d2 if d2 > 0 else 0
+        return self._statistic('dispersion_y')
+
+    def alpha_Twiss_x(self):
+        return self._statistic('alpha_Twiss_x')
+
+    def alpha_Twiss_y(self):
+        return self._statistic('alpha_Twiss_y')
+
+    def beta_Twiss_x(self):
+        return self._statistic('beta_Twiss_x')
+
+    def beta_Twiss_y(self):
+        return self._statistic('beta_Twiss_y')
+
+    def gamma_Twiss_x(self):
+        return self._statistic('gamma_Twiss_x')
+
+    def gamma_Twiss_y(self):
+        return self._statistic('gamma_Twiss_y')

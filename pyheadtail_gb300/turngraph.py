@@ -109,3 +109,4 @@ class TurnGraph(object):
             self.capture()
         for _ in range(n_graphs):
             self.graph.replay()
+        self.beam._engine.touch()

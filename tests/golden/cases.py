@@ -79,6 +79,18 @@ def probe(sl, statistics=('mean_x', 'mean_y')):
     return dict(type='probe', slicer=sl, statistics=list(statistics))
 
 
+# every statistic of Particles (particles/particles.py:311-390); a case
+# lists the ones recorded for the bunch after each recorded turn in
+# record_bunch_stats
+BUNCH_STATS = [
+    'mean_x', 'mean_xp', 'mean_y', 'mean_yp', 'mean_z', 'mean_dp',
+    'sigma_x', 'sigma_y', 'sigma_z', 'sigma_xp', 'sigma_yp', 'sigma_dp',
+    'effective_normalized_emittance_x', 'effective_normalized_emittance_y',
+    'effective_normalized_emittance_z', 'epsn_x', 'epsn_y', 'epsn_z',
+    'dispersion_x', 'dispersion_y', 'alpha_Twiss_x', 'alpha_Twiss_y',
+    'beta_Twiss_x', 'beta_Twiss_y', 'gamma_Twiss_x', 'gamma_Twiss_y']
+
+
 # the C1 and C2 workloads at fixture size (full sizes are in bench.py)
 CASES = {
     'transverse_linear': dict(
@@ -143,6 +155,15 @@ CASES = {
         beam=beam_params(1000, 22), n_turns=3,
         elements=[smooth_transverse(), linear_map(),
                   wake(slicer(25), resonator(kind='parallel_horizontal'),
+                       resonator(R=3e6, f=0.6e9, Q=0.5,
+                                 kind='longitudinal'))]),
+    # dispersion from the RF kick (D_x), dipolar, quadrupolar and
+    # longitudinal wake kicks: every statistic of the bunch after the wake
+    'bunch_statistics': dict(
+        beam=beam_params(1500, 23, alpha_x=0.4, alpha_y=-0.3), n_turns=3,
+        record_bunch_stats=BUNCH_STATS,
+        elements=[smooth_transverse(chroma=[3., -2.]), rf(D_x=0.7, D_y=0.2),
+                  wake(slicer(40), resonator(kind='parallel_horizontal'),
                        resonator(R=3e6, f=0.6e9, Q=0.5,
                                  kind='longitudinal'))]),
     'c1_full': dict(

@@ -116,6 +116,9 @@ def run(spec, beam, n_turns=None, record_turns=None):
                 for st in stats:
                     rec[p + st] = _np(getattr(ss, st))
         if turn in record_turns:
+            # statistics first: they see the wake kicks still pending
+            for st in spec.get('record_bunch_stats', ()):
+                rec['t%d_bs_%s' % (turn, st)] = np.float64(getattr(beam, st)())
             c = beam.coords_numpy()
             for k in COORDS:
                 rec['t%d_%s' % (turn, k)] = c[k]

@@ -57,6 +57,9 @@ def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9, emit_rtol=1e-7,
             continue
         assert k in rec, '%s: missing %s' % (label, k)
         g = rec[k]
+        if '_bs_' in k:
+            compare_bunch_stat(rec, ref, k, label)
+            continue
         if k.endswith('_z_bins') and bins_rtol > 0:
             np.testing.assert_allclose(g, v, rtol=0, atol=bins_rtol *
                                        np.max(np.abs(v)), err_msg=k)
@@ -79,6 +82,22 @@ def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9, emit_rtol=1e-7,
                    emit_rtol if 'epsn' in k else stat_rtol)
             e = rms_err(g[ok], v[ok])
             assert e <= tol, '%s %s: rel err %.3g' % (label, k, e)
+
+
+# bunch statistics (Particles.mean_* ... gamma_Twiss_*): the GPU sums in a
+# tree what the reference sums sequentially (np.mean pairwise), so they
+# agree to rounding; centroids are compared relative to the spread of the
+# coordinate, since a centroid near zero has no relative precision
+BUNCH_STAT_RTOL = 1e-12
+
+
+def compare_bunch_stat(rec, ref, k, label, rtol=BUNCH_STAT_RTOL):
+    g, v = float(rec[k]), float(ref[k])
+    turn, name = k.split('_bs_')
+    scale = abs(v)
+    if name.startswith('mean_'):
+        scale = max(scale, float(ref['%s_bs_sigma_%s' % (turn, name[5:])]))
+    assert abs(g - v) <= rtol * scale, '%s %s: %r vs %r' % (label, k, g, v)
 
 
 def load(path):

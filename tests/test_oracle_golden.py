@@ -3,7 +3,8 @@ reference (tests/golden/make_golden.py).
 
 The oracle restates the reference's NumPy/Cython arithmetic in the same
 operation order, so everything is compared bit for bit: coordinates, beam
-scalars, slice indices, counts, bins and per-slice statistics.
+scalars, slice indices, counts, bins, per-slice statistics and every bunch
+statistic of Particles (``bunch_statistics``).
 """
 import glob
 import json
@@ -48,5 +49,6 @@ def test_fixture_set_covers_every_stage():
     for need in ('transverse_chroma_amp', 'transverse_segments_dispersion',
                  'linear_map', 'rf_double_harmonic', 'rf_accelerating',
                  'slicer_fixed', 'wake_resonator', 'wake_multiturn',
-                 'wake_dynamic_cuts', 'wake_plates', 'c1_full', 'c2_full'):
+                 'wake_dynamic_cuts', 'wake_plates', 'c1_full', 'c2_full',
+                 'bunch_statistics'):
         assert need in names
