@@ -1,5 +1,7 @@
 """Build and run oracle objects from a case specification dict (the schema
 of ``tests/golden/cases.py``).  Test infrastructure only."""
+import os
+
 import numpy as np
 from scipy.constants import e, m_p
 
@@ -16,6 +18,12 @@ def make_beam(bp, coords=None):
                                 bp['alpha_x'], bp['alpha_y'])
     return T.Beam(coords, bp['intensity'] / bp['n'], e, m_p,
                   bp['circumference'], bp['gamma'])
+
+
+def table_path(name):
+    """Wake tables of the cases live beside the golden fixtures."""
+    return os.path.join(os.path.dirname(os.path.dirname(
+        os.path.abspath(__file__))), 'tests', 'golden', name)
 
 
 def make_slicer(sp):
@@ -51,6 +59,17 @@ def make_kicks(src, slicer):
         if Z:
             kicks.append(T.WakeKick(T.resonator_longitudinal(R, f, Q),
                                     slicer, ntw, 'dp', None))
+        return kicks
+    if src['type'] == 'wake_table':
+        table = T.load_wake_table(table_path(src['file']), src['columns'])
+        kicks = []
+        for name, target, moment, quad in T.TABLE_KICKS:
+            if name not in table:
+                continue
+            wf = (T.table_longitudinal(table) if name == 'longitudinal'
+                  else T.table_transverse(table, name))
+            kicks.append(T.WakeKick(wf, slicer, ntw, target, moment,
+                                    quad=quad))
         return kicks
     if src['type'] == 'resistive_wall':
         wf = T.resistive_wall_transverse(src['b'], src['L'], src['sigma'],

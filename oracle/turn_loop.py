@@ -790,6 +790,61 @@ def resistive_wall_transverse(pipe_radius, length, conductivity, dt_min,
     return wake
 
 
+def load_wake_table(wake_file, wake_file_columns):
+    """WakeTable.__init__, impedances/wakes.py:201-217: columns by name."""
+    data = np.loadtxt(wake_file)
+    if len(wake_file_columns) != data.shape[1]:
+        raise ValueError('wake_file_columns does not match the table')
+    return {name: data[:, i] for i, name in enumerate(wake_file_columns)}
+
+
+def table_transverse(table, component):
+    """WakeTable.function_transverse, wakes.py:298-339: linear
+    interpolation (scipy interp1d) of the table in SI units with the
+    HEADTAIL sign; ultrarelativistic tables clip dt to <= 0."""
+    from scipy.interpolate import interp1d
+    time = 1e-9 * table['time']
+    strength = -1e15 * table[component]
+    f = interp1d(time, strength)
+    if time[0] == 0 and strength[0] == 0:
+        def wake(dt, *args, **kwargs):
+            return f(-dt.clip(max=0))
+    elif time[0] < 0:
+        def wake(dt, *args, **kwargs):
+            return f(-dt)
+    else:
+        raise ValueError(component + ' does not meet requirements.')
+    return wake
+
+
+def table_longitudinal(table):
+    """WakeTable.function_longitudinal, wakes.py:341-376."""
+    from scipy.interpolate import interp1d
+    time = 1e-9 * table['time']
+    strength = 1e12 * table['longitudinal']
+    f = interp1d(time, strength, bounds_error=False, fill_value=0.)
+
+    def wake(dt, *args, **kwargs):
+        w = f(-dt)
+        if time[0] == 0:
+            return (np.sign(-dt) + 1.) / 2. * w
+        if time[0] < 0:
+            return w
+        raise ValueError('longitudinal component does not meet requirements')
+    return wake
+
+
+# WakeTable.get_wake_kicks order (wakes.py:219-285): component, target,
+# moment (None: count), quadrupolar coordinate
+TABLE_KICKS = [('constant_x', 'xp', None, None), ('constant_y', 'yp', None, None),
+               ('longitudinal', 'dp', None, None),
+               ('dipole_x', 'xp', 'x', None), ('dipole_y', 'yp', 'y', None),
+               ('dipole_xy', 'xp', 'y', None), ('dipole_yx', 'yp', 'x', None),
+               ('quadrupole_x', 'xp', None, 'x'), ('quadrupole_y', 'yp', None, 'y'),
+               ('quadrupole_xy', 'xp', None, 'y'),
+               ('quadrupole_yx', 'yp', None, 'x')]
+
+
 class WakeKick(object):
     """WakeKick base + dipole/quadrupole/constant kicks,
     wake_kicks.py:19-139, 144-361.

@@ -14,7 +14,8 @@ its variants (:627-678), same constructors and the same
   3. ``phk_wake``: every kick's multi-turn convolution on the device (FP32
      form: ``phk_wake_tc_run``, a BF16x3 Toeplitz GEMM on the tensor cores)
   4. the kicks are left pending on the beam (applied by the next pass).
-``WakeTable`` (tabulated wakes) is not part of this package.
+``WakeTable`` (:167-376) samples tabulated wakes with the reference's
+interpolation on the host; the device work is the same.
 """
 import ctypes
 from abc import ABCMeta, abstractmethod
@@ -416,3 +417,109 @@ class ParallelVerticalPlatesResistiveWall(ResistiveWall):
             pipe_radius, resistive_wall_length, conductivity, dt_min,
             np.pi**2 / 12., np.pi**2 / 24., np.pi**2 / 24., -np.pi**2 / 24.,
             n_turns_wake, *args, **kwargs)
+
+
+class WakeTable(WakeSource):
+    """Wakes from a table (wakes.py:167-376): the same file format and
+    column names, the same get_wake_kicks order, and the reference's
+    linear interpolation (scipy interp1d of the table converted to SI
+    units and HEADTAIL signs), evaluated on the host into the device
+    tables of the convolution.
+
+    Columns (``wake_file_columns``, in file order): 'time' [ns] and any of
+    'constant_x', 'constant_y', 'dipole_x', 'dipole_y', 'dipole_xy',
+    'dipole_yx', 'quadrupole_x', 'quadrupole_y', 'quadrupole_xy',
+    'quadrupole_yx' [V/pC/mm] and 'longitudinal' [V/pC].  A table whose
+    first time is 0 (with transverse values 0 there) is an
+    ultrarelativistic wake, clipped to dt <= 0; a table starting at
+    negative times is a low-beta wake.  Transverse samples outside the
+    table raise ValueError (interp1d), longitudinal ones are 0.
+    One difference: the reference appends a 'quadrupole_xy' kick to a
+    list that does not exist (wakes.py:274-277) and so raises; here the
+    kick is created like the others."""
+
+    def __init__(self, wake_file, wake_file_columns, n_turns_wake=1, *args,
+                 **kwargs):
+        self.wake_table = {}
+        wake_data = np.loadtxt(wake_file)
+        if len(wake_file_columns) != wake_data.shape[1]:
+            raise ValueError('Length of wake_file_columns list does not '
+                             'correspond to the number of columns in the '
+                             'specified wake_file. \n')
+        if 'time' not in wake_file_columns:
+            raise ValueError("No wake_file_column with name 'time' has "
+                             'been specified. \n')
+        for i, column_name in enumerate(wake_file_columns):
+            self.wake_table[column_name] = wake_data[:, i]
+        self.n_turns_wake = n_turns_wake
+
+    def get_wake_kicks(self, slicer):
+        """wakes.py:219-285."""
+        from .wake_kicks import (ConstantWakeKickX, ConstantWakeKickY,
+                                 DipoleWakeKickXY, DipoleWakeKickYX,
+                                 QuadrupoleWakeKickXY, QuadrupoleWakeKickYX)
+        n = self.n_turns_wake
+        order = [('constant_x', ConstantWakeKickX),
+                 ('constant_y', ConstantWakeKickY),
+                 ('longitudinal', ConstantWakeKickZ),
+                 ('dipole_x', DipoleWakeKickX),
+                 ('dipole_y', DipoleWakeKickY),
+                 ('dipole_xy', DipoleWakeKickXY),
+                 ('dipole_yx', DipoleWakeKickYX),
+                 ('quadrupole_x', QuadrupoleWakeKickX),
+                 ('quadrupole_y', QuadrupoleWakeKickY),
+                 ('quadrupole_xy', QuadrupoleWakeKickXY),
+                 ('quadrupole_yx', QuadrupoleWakeKickYX)]
+        kicks = []
+        for name, cls in order:
+            if not self._is_provided(name):
+                continue
+            wf = (self.function_longitudinal() if name == 'longitudinal'
+                  else self.function_transverse(name))
+            kicks.append(cls(wf, slicer, n))
+        return kicks
+
+    def _is_provided(self, wake_component):
+        return wake_component in self.wake_table
+
+    def function_transverse(self, wake_component):
+        """wakes.py:298-339."""
+        from scipy.interpolate import interp1d
+        convert_to_s = 1e-9
+        convert_to_V_per_Cm = 1e15
+        time = convert_to_s * self.wake_table['time']
+        wake_strength = -convert_to_V_per_Cm * self.wake_table[wake_component]
+        interpolation_function = interp1d(time, wake_strength)
+        if (time[0] == 0) and (wake_strength[0] == 0):
+            def wake(dt, *args, **kwargs):
+                dt = dt.clip(max=0)
+                return interpolation_function(-dt)
+            self.prints(wake_component + ' Assuming ultrarelativistic wake.')
+        elif time[0] < 0:
+            def wake(dt, *args, **kwargs):
+                return interpolation_function(-dt)
+            self.prints(wake_component + ' Found low beta wake.')
+        else:
+            raise ValueError(wake_component + ' does not meet requirements.')
+        return wake
+
+    def function_longitudinal(self):
+        """wakes.py:341-376 (beam loading theorem: half the value at
+        dt = 0 for tables starting at 0)."""
+        from scipy.interpolate import interp1d
+        convert_to_s = 1e-9
+        convert_to_V_per_C = 1e12
+        time = convert_to_s * self.wake_table['time']
+        wake_strength = convert_to_V_per_C * self.wake_table['longitudinal']
+        interpolation_function = interp1d(time, wake_strength,
+                                          bounds_error=False, fill_value=0.)
+
+        def wake(dt, *args, **kwargs):
+            wake_interpolated = interpolation_function(-dt)
+            if time[0] == 0:
+                return (np.sign(-dt) + 1.) / 2. * wake_interpolated
+            elif time[0] < 0:
+                return wake_interpolated
+            raise ValueError('Longitudinal wake component does not meet '
+                             'requirements.')
+        return wake

@@ -69,6 +69,18 @@ def resistive_wall(b=0.02, L=C_SPS, sigma=5.8e7, dt_min=1e-12,
                 dt_min=dt_min, n_turns_wake=n_turns_wake)
 
 
+TABLE_COLUMNS = ['time', 'constant_x', 'dipole_x', 'dipole_y', 'dipole_xy',
+                 'dipole_yx', 'quadrupole_x', 'quadrupole_y', 'longitudinal']
+
+
+def wake_table(file='wake_table_ultra.dat', columns=TABLE_COLUMNS,
+               n_turns_wake=1):
+    """A WakeTable source; ``file`` lives in this directory (synthetic
+    tables written by make_wake_tables.py)."""
+    return dict(type='wake_table', file=file, columns=list(columns),
+                n_turns_wake=n_turns_wake)
+
+
 def wake(sl, *sources):
     return dict(type='wake', slicer=sl, sources=list(sources))
 
@@ -166,6 +178,17 @@ CASES = {
                   wake(slicer(40), resonator(kind='parallel_horizontal'),
                        resonator(R=3e6, f=0.6e9, Q=0.5,
                                  kind='longitudinal'))]),
+    # tabulated wakes: every kick kind (constant, dipolar, cross dipolar,
+    # quadrupolar, longitudinal) from one table, multi-turn; and a
+    # low-beta table
+    'wake_table_multiturn': dict(
+        beam=beam_params(1200, 24), n_turns=5,
+        elements=[smooth_transverse(chroma=[1., 1.]), rf(),
+                  wake(slicer(40), wake_table(n_turns_wake=3))]),
+    'wake_table_lowbeta': dict(
+        beam=beam_params(1200, 25), n_turns=3,
+        elements=[smooth_transverse(), linear_map(),
+                  wake(slicer(30), wake_table('wake_table_lowbeta.dat'))]),
     'c1_full': dict(
         beam=beam_params(1000, 0), n_turns=5,
         elements=[smooth_transverse(), linear_map(),

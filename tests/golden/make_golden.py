@@ -85,6 +85,10 @@ def make_source(src):
                                    Yokoya_X2=0, Yokoya_Y2=0, switch_Z=True,
                                    n_turns_wake=src['n_turns_wake'],
                                    printer=sp, warningprinter=sp)
+    if src['type'] == 'wake_table':
+        return wakes.WakeTable(os.path.join(HERE, src['file']), src['columns'],
+                               n_turns_wake=src['n_turns_wake'], printer=sp,
+                               warningprinter=sp)
     if src['type'] == 'resistive_wall' and src['kind'] == 'circular':
         return wakes.CircularResistiveWall(
             src['b'], src['L'], src['sigma'], src['dt_min'],

@@ -38,6 +38,12 @@ def make_source(src):
         if src['kind'] == 'longitudinal':
             return W.Resonator(*args, Yokoya_X1=0, Yokoya_Y1=0, Yokoya_X2=0,
                                Yokoya_Y2=0, switch_Z=True, n_turns_wake=ntw)
+    if src['type'] == 'wake_table':
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                            'golden', src['file'])
+        return W.WakeTable(path, src['columns'], n_turns_wake=ntw,
+                           printer=SP)
     if src['type'] == 'resistive_wall' and src['kind'] == 'circular':
         return W.CircularResistiveWall(src['b'], src['L'], src['sigma'],
                                        src['dt_min'], n_turns_wake=ntw)

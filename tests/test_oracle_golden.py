@@ -50,5 +50,6 @@ def test_fixture_set_covers_every_stage():
                  'linear_map', 'rf_double_harmonic', 'rf_accelerating',
                  'slicer_fixed', 'wake_resonator', 'wake_multiturn',
                  'wake_dynamic_cuts', 'wake_plates', 'c1_full', 'c2_full',
-                 'bunch_statistics'):
+                 'bunch_statistics', 'wake_table_multiturn',
+                 'wake_table_lowbeta'):
         assert need in names
