@@ -99,6 +99,7 @@ typedef struct phk_slicer {
 #define PHK_OP_RF_KICK 3      /* Kick.track_*, longitudinal_tracking.py:183-203           */
 #define PHK_OP_LINEAR_LONG 4  /* LinearMap.track_*, longitudinal_tracking.py:731-759      */
 #define PHK_OP_SCALE_TRANS 5  /* RFSystems._shrink_transverse_emittance, :546-554         */
+#define PHK_OP_DAMPER 6       /* TransverseDamper.track_*, feedback/transverse_damper.py:64-86 */
 
 /* op flags */
 #define PHK_FLAG_DISPERSION 1 /* subtract / add D * dp around the op      */
@@ -107,6 +108,9 @@ typedef struct phk_slicer {
 #define PHK_FLAG_PHI_OFFSET 8 /* rf kick: add phi_offset                  */
 #define PHK_FLAG_PHI_LOCK 16  /* rf kick: add _phi_lock                   */
 #define PHK_FLAG_P_INC 32     /* rf kick: subtract p_increment            */
+#define PHK_FLAG_DAMP_X 64    /* damper: horizontal plane active          */
+#define PHK_FLAG_DAMP_Y 128   /* damper: vertical plane active            */
+#define PHK_FLAG_REACTIVE 256 /* damper: local beta given (reactive part) */
 
 /*
  * phk_op.p layout per kind (all FP64):
@@ -129,6 +133,12 @@ typedef struct phk_slicer {
  *  LINEAR_LONG:  p[0] = cos(2 pi Q_s), p[1] = sin(2 pi Q_s), p[2] = longfac,
  *                p[3] = D_x, p[4] = D_y, p[5] = 1/longfac
  *  SCALE_TRANS:  p[0] = sqrt(betagamma_old / betagamma_new)
+ *  DAMPER:       p[0] = gain_x sin(phase), p[1] = gain_x cos(phase),
+ *                p[2] = local beta, p[3..5] the same for y; the eight bytes
+ *                of p[31] hold a device pointer to the bunch means
+ *                (phk_stats.means, written before the pass runs):
+ *                xp -= p[0] * <xp>, then (REACTIVE) xp -= p[1] * <x> / p[2];
+ *                the same for y, yp
  *
  * With PHK_F32 coordinates the same 256 bytes hold 64 floats; hi/lo pairs
  * are float-float values (hi + lo), fractions in turns have the integer part
@@ -148,6 +158,7 @@ typedef struct phk_slicer {
  *  LINEAR_LONG:  f[0..1] cos hi/lo, f[2..3] longfac * sin hi/lo, f[4..5]
  *                D_x, D_y, f[6..7] sin / longfac hi/lo
  *  SCALE_TRANS:  f[0]
+ *  DAMPER:       f[0..5] as p[0..5]; p[31] as above (the float means)
  * and phk_detuner.c holds 32 floats: CHROMA as above (x from f[0], y from
  * f[8]); AMPLITUDE f[0..3] = dapp / p0, f[4..9] as above.
  */
@@ -373,6 +384,9 @@ typedef struct phk_stats {
     double *partials;  /* device workspace [grid][PHK_STATS_LEN]          */
     uint32_t *ticket;  /* device word; zero before the first call, and
                           every call leaves it zero                        */
+    double *means;     /* optional device [6] doubles then [6] floats:
+                          shift_q + S_q / n of the summed coordinates (0
+                          for the others), in FP64 and rounded to FP32   */
     int32_t grid;      /* phk_bunch_stats_grid(n, dtype)                   */
     int32_t mask;      /* coordinates to sum (bit q = PHK_X ... PHK_DP; 0:
                           all six); sums of the others are written as 0  */

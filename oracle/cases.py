@@ -114,6 +114,10 @@ def make_elements(spec, beam):
         elif t == 'probe':
             out.append(('probe', (make_slicer(el['slicer']),
                                   el['statistics'])))
+        elif t == 'damper':
+            out.append(('map', T.TransverseDamper(
+                el['dampingrate_x'], el['dampingrate_y'], el['phase'],
+                el['local_beta'])))
         else:
             raise ValueError(t)
     return out

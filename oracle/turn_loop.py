@@ -790,6 +790,31 @@ def resistive_wall_transverse(pipe_radius, length, conductivity, dt_min,
     return wake
 
 
+class TransverseDamper(object):
+    """Ideal transverse damper, feedback/transverse_damper.py:17-86."""
+
+    def __init__(self, dampingrate_x, dampingrate_y, phase=90,
+                 local_beta_function=None):
+        self.gain_x = 2 / dampingrate_x if dampingrate_x else None
+        self.gain_y = 2 / dampingrate_y if dampingrate_y else None
+        self.phase_in_2pi = phase / 360. * 2 * np.pi
+        self.local_beta_function = local_beta_function
+
+    def track(self, beam):
+        # track_all's order (:77-86); one plane: track_horizontal/_vertical
+        if self.gain_x is not None:
+            beam.xp -= self.gain_x * np.sin(self.phase_in_2pi) * beam.mean_xp()
+        if self.gain_y is not None:
+            beam.yp -= self.gain_y * np.sin(self.phase_in_2pi) * beam.mean_yp()
+        if self.local_beta_function:
+            if self.gain_x is not None:
+                beam.xp -= (self.gain_x * np.cos(self.phase_in_2pi) *
+                            beam.mean_x() / self.local_beta_function)
+            if self.gain_y is not None:
+                beam.yp -= (self.gain_y * np.cos(self.phase_in_2pi) *
+                            beam.mean_y() / self.local_beta_function)
+
+
 def load_wake_table(wake_file, wake_file_columns):
     """WakeTable.__init__, impedances/wakes.py:201-217: columns by name."""
     data = np.loadtxt(wake_file)

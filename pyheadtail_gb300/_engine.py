@@ -153,12 +153,13 @@ class Op(object):
     form) the float parameters packed into the same 256 bytes."""
 
     def __init__(self, kind, flags=0, p=None, pf=None, detuners=(),
-                 ij_mask=0):
+                 ij_mask=0, pointer=None):
         self.kind, self.flags = kind, flags
         self.p = p or {}
         self.pf = pf or {}
         self.detuners = list(detuners)   # list of (DetunerPack)
         self.ij_mask = ij_mask
+        self.pointer = pointer           # device address stored in p[31]
 
     def pack(self, st, code, det_begin):
         st.kind = self.kind
@@ -174,6 +175,10 @@ class Op(object):
             for k, v in self.pf.items():
                 buf[k] = v
             ctypes.memmove(ctypes.addressof(st.p), buf.ctypes.data, 256)
+        if self.pointer is not None:
+            ptr = ctypes.c_uint64(self.pointer)
+            ctypes.memmove(ctypes.addressof(st.p) + 248, ctypes.addressof(ptr),
+                           8)
 
 
 class DetunerPack(object):

@@ -23,8 +23,10 @@ COORD_INDEX = {'x': PHK_X, 'xp': PHK_XP, 'y': PHK_Y, 'yp': PHK_YP,
                'z': PHK_Z, 'dp': PHK_DP}
 
 OP_TRANSVERSE, OP_DRIFT, OP_RF_KICK, OP_LINEAR_LONG, OP_SCALE_TRANS = 1, 2, 3, 4, 5
+OP_DAMPER = 6
 FLAG_DISPERSION, FLAG_DETUNED, FLAG_SHRINK = 1, 2, 4
 FLAG_PHI_OFFSET, FLAG_PHI_LOCK, FLAG_P_INC = 8, 16, 32
+FLAG_DAMP_X, FLAG_DAMP_Y, FLAG_REACTIVE = 64, 128, 256
 DET_CHROMA, DET_AMPLITUDE = 1, 2
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
@@ -135,6 +137,7 @@ class Stats(ctypes.Structure):
     _fields_ = [('order', ctypes.c_int32), ('capacity', ctypes.c_int32),
                 ('records', ctypes.c_void_p), ('cursor', ctypes.c_void_p),
                 ('partials', ctypes.c_void_p), ('ticket', ctypes.c_void_p),
+                ('means', ctypes.c_void_p),
                 ('grid', ctypes.c_int32), ('mask', ctypes.c_int32)]
 
 

@@ -96,9 +96,16 @@ static int check_program(const phk_program* p, const char* who) {
                          p->n_det, PHK_MAX_DETUNERS);
     for (int o = 0; o < p->n_ops; ++o) {
         const phk_op& op = p->op[o];
-        if (op.kind < PHK_OP_TRANSVERSE || op.kind > PHK_OP_SCALE_TRANS)
+        if (op.kind < PHK_OP_TRANSVERSE || op.kind > PHK_OP_DAMPER)
             return set_error(PHK_EPARAM, "%s: op %d has unknown kind %d", who,
                              o, op.kind);
+        if (op.kind == PHK_OP_DAMPER) {
+            uint64_t ptr;
+            memcpy(&ptr, &op.p[31], sizeof(ptr));
+            if (!ptr || ptr % 8)
+                return set_error(PHK_EPARAM, "%s: damper op %d has no aligned "
+                                 "means pointer", who, o);
+        }
         if (op.kind == PHK_OP_TRANSVERSE && (op.flags & PHK_FLAG_DETUNED)) {
             if (op.det_begin < 0 || op.det_count < 0 ||
                 op.det_begin + op.det_count > p->n_det)
@@ -490,7 +497,8 @@ int phk_bunch_stats(const phk_coords* coords, const phk_kick_set* pending,
     if (reinterpret_cast<uintptr_t>(s.records) % 8 ||
         reinterpret_cast<uintptr_t>(s.partials) % 8 ||
         reinterpret_cast<uintptr_t>(s.cursor) % 8 ||
-        reinterpret_cast<uintptr_t>(s.ticket) % 4)
+        reinterpret_cast<uintptr_t>(s.ticket) % 4 ||
+        reinterpret_cast<uintptr_t>(s.means) % 8)
         return set_error(PHK_EALIGN, "%s: a workspace pointer is misaligned",
                          who);
     return launch_stats(coords, pending, stats, (cudaStream_t)stream);

@@ -53,6 +53,7 @@ __host__ __device__ constexpr int pair_entry(int a, int b) {
 struct StatsOut {
     double* partials;   // [grid][PHK_STATS_LEN]
     double* records;    // [capacity][PHK_STATS_LEN]
+    double* means;      // optional [6] doubles + [6] floats
     int64_t* cursor;
     uint32_t* ticket;
     int64_t n;
@@ -133,6 +134,13 @@ __device__ __forceinline__ void merge_rows(const StatsOut& o,
     if (tid < 6) rec[1 + tid] = shift[tid];
     if (tid == 0) rec[0] = (double)o.n;
     __syncthreads();
+    if (o.means && tid < 6) {
+        const double m = ((o.entries >> (7 + tid)) & 1) && o.n > 0
+                             ? __dadd_rn(rec[1 + tid], __ddiv_rn(rec[7 + tid], (double)o.n))
+                             : 0.0;
+        o.means[tid] = m;
+        reinterpret_cast<float*>(o.means + 6)[tid] = (float)m;
+    }
     if (tid == 0) {
         *o.ticket = 0u;
         if (o.cursor) *o.cursor = c + 1;
@@ -379,6 +387,7 @@ static StatsOut stats_out(const phk_coords* c, const phk_stats* s) {
     StatsOut o;
     o.partials = s->partials;
     o.records = s->records;
+    o.means = s->means;
     o.cursor = s->cursor;
     o.ticket = s->ticket;
     o.n = c->n;

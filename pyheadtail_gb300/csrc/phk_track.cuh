@@ -236,6 +236,35 @@ __device__ __forceinline__ void op_scale(const phk_op& op,
         for (int q = 0; q < 4; ++q) t.c[q][j] = mul(t.c[q][j], f);
 }
 
+// the device means a damper op reads (phk_stats.means, FP64 then FP32)
+__device__ __forceinline__ const double* damper_means(const phk_op& op) {
+    unsigned long long bits;
+    memcpy(&bits, &op.p[31], sizeof(bits));
+    return reinterpret_cast<const double*>(bits);
+}
+
+// TransverseDamper.track_all (feedback/transverse_damper.py:64-86): the
+// reference's order, xp -= (g sin) <xp>, then xp -= ((g cos) <x>) / beta
+template <int VEC>
+__device__ __forceinline__ void op_damper(const phk_op& op,
+                                          Tile<double, VEC>& t) {
+    const double* m = damper_means(op);
+    const bool reactive = op.flags & PHK_FLAG_REACTIVE;
+#pragma unroll
+    for (int pl = 0; pl < 2; ++pl) {
+        if (!(op.flags & (pl == 0 ? PHK_FLAG_DAMP_X : PHK_FLAG_DAMP_Y))) continue;
+        const int u = pl == 0 ? PHK_X : PHK_Y, up = pl == 0 ? PHK_XP : PHK_YP;
+        const double* g = op.p + 3 * pl;
+        const double c1 = mul(g[0], __ldg(m + up));
+        const double c2 = reactive ? __ddiv_rn(mul(g[1], __ldg(m + u)), g[2]) : 0.0;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            t.c[up][j] = __dsub_rn(t.c[up][j], c1);
+            if (reactive) t.c[up][j] = __dsub_rn(t.c[up][j], c2);
+        }
+    }
+}
+
 // ===================================================================
 // element arithmetic, FP32 precision form (parameters packed as floats)
 // ===================================================================
@@ -423,6 +452,27 @@ __device__ __forceinline__ void op_scale(const phk_op& op,
         for (int q = 0; q < 4; ++q) t.c[q][j] *= f;
 }
 
+template <int VEC>
+__device__ __forceinline__ void op_damper(const phk_op& op,
+                                          Tile<float, VEC>& t) {
+    const float* m = reinterpret_cast<const float*>(damper_means(op) + 6);
+    const float* f = reinterpret_cast<const float*>(op.p);
+    const bool reactive = op.flags & PHK_FLAG_REACTIVE;
+#pragma unroll
+    for (int pl = 0; pl < 2; ++pl) {
+        if (!(op.flags & (pl == 0 ? PHK_FLAG_DAMP_X : PHK_FLAG_DAMP_Y))) continue;
+        const int u = pl == 0 ? PHK_X : PHK_Y, up = pl == 0 ? PHK_XP : PHK_YP;
+        const float* g = f + 3 * pl;
+        const float c1 = g[0] * __ldg(m + up);
+        const float c2 = reactive ? __fdiv_rn(g[1] * __ldg(m + u), g[2]) : 0.f;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            t.c[up][j] -= c1;
+            if (reactive) t.c[up][j] -= c2;
+        }
+    }
+}
+
 // one dispatch per op per tile (uniform across the CTA)
 template <typename T, int VEC>
 __device__ __forceinline__ void run_program(const phk_program& prog,
@@ -435,6 +485,7 @@ __device__ __forceinline__ void run_program(const phk_program& prog,
             case PHK_OP_RF_KICK: op_rfkick<VEC>(op, t); break;
             case PHK_OP_LINEAR_LONG: op_linear_long<VEC>(op, t); break;
             case PHK_OP_SCALE_TRANS: op_scale<VEC>(op, t); break;
+            case PHK_OP_DAMPER: op_damper<VEC>(op, t); break;
             default: break;
         }
     }
@@ -1360,6 +1411,10 @@ static inline int op_mask(const phk_program* prog, int* load, int* store) {
                 break;
             case PHK_OP_SCALE_TRANS:
                 ld |= 0x0F; stm |= 0x0F;
+                break;
+            case PHK_OP_DAMPER:
+                if (op.flags & PHK_FLAG_DAMP_X) { ld |= 0x03; stm |= 0x02; }
+                if (op.flags & PHK_FLAG_DAMP_Y) { ld |= 0x0C; stm |= 0x08; }
                 break;
         }
     }

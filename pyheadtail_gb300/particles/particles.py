@@ -240,9 +240,10 @@ class Particles(Printing):
         return self._stats_ws
 
     def stats_struct(self, records, capacity=1, cursor=None, order=2,
-                     mask=0x3f):
+                     mask=0x3f, means=None):
         """phk_stats for a statistics pass of this bunch into ``records``
-        (a float64 CUDA tensor of capacity * 34 entries)."""
+        (a float64 CUDA tensor of capacity * 34 entries); ``means`` (a
+        float64 CUDA tensor of 9 entries) receives the device means."""
         grid, part, ticket, _ = self._stats_workspace()
         st = N.Stats()
         st.order = order
@@ -251,17 +252,18 @@ class Particles(Printing):
         st.cursor = 0 if cursor is None else cursor.data_ptr()
         st.partials = part.data_ptr()
         st.ticket = ticket.data_ptr()
+        st.means = 0 if means is None else means.data_ptr()
         st.grid = grid
         st.mask = mask
         return st
 
     def launch_stats(self, records, capacity=1, cursor=None, order=2,
-                     mask=0x3f):
+                     mask=0x3f, means=None):
         """Queue one statistics pass of the current state (no sync)."""
         eng = self._engine
         if eng.ops:
             eng.flush()
-        st = self.stats_struct(records, capacity, cursor, order, mask)
+        st = self.stats_struct(records, capacity, cursor, order, mask, means)
         coords = eng.coords_struct()
         ks = eng.kick.struct() if eng.kick is not None else None
         N.call('phk_bunch_stats', ctypes.byref(coords),

@@ -81,6 +81,13 @@ def wake_table(file='wake_table_ultra.dat', columns=TABLE_COLUMNS,
                 n_turns_wake=n_turns_wake)
 
 
+def damper(dampingrate_x=50., dampingrate_y=50., phase=90, local_beta=None):
+    """TransverseDamper (feedback/transverse_damper.py:15-94)."""
+    return dict(type='damper', dampingrate_x=dampingrate_x,
+                dampingrate_y=dampingrate_y, phase=phase,
+                local_beta=local_beta)
+
+
 def wake(sl, *sources):
     return dict(type='wake', slicer=sl, sources=list(sources))
 
@@ -189,6 +196,17 @@ CASES = {
         beam=beam_params(1200, 25), n_turns=3,
         elements=[smooth_transverse(), linear_map(),
                   wake(slicer(30), wake_table('wake_table_lowbeta.dat'))]),
+    # the damper after a wake (its means see the kicks), a resistive one
+    # in both planes and a reactive one in one plane before the maps
+    'damper_resistive': dict(
+        beam=beam_params(1200, 26), n_turns=4,
+        elements=[smooth_transverse(chroma=[2., 2.]), rf(),
+                  wake(slicer(40), resonator()), damper(20., 30.)]),
+    'damper_reactive': dict(
+        beam=beam_params(1200, 27), n_turns=4,
+        elements=[damper(25., 0., phase=60., local_beta=50.),
+                  smooth_transverse(), linear_map(),
+                  wake(slicer(40), resonator())]),
     'c1_full': dict(
         beam=beam_params(1000, 0), n_turns=5,
         elements=[smooth_transverse(), linear_map(),

@@ -85,6 +85,12 @@ def make_elements(spec, beam):
         elif t == 'probe':
             out.append(('probe', (make_slicer(el['slicer']),
                                   el['statistics'])))
+        elif t == 'damper':
+            from pyheadtail_gb300.feedback.transverse_damper import \
+                TransverseDamper
+            out.append(('map', TransverseDamper(
+                el['dampingrate_x'], el['dampingrate_y'], phase=el['phase'],
+                local_beta_function=el['local_beta'], printer=SP)))
         else:
             raise ValueError(t)
     return out

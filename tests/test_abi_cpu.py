@@ -97,6 +97,46 @@ def test_struct_layout_matches_header():
     assert ctypes.sizeof(N.Accum) == 80
     assert ctypes.sizeof(N.WakeKick) == 40
     assert N.WakeSet.kick.offset == 32
+    assert ctypes.sizeof(N.Stats) == 56
+    assert N.Stats.means.offset == 40
+
+
+def test_stats_and_damper_validation_without_gpu(lib):
+    """phk_bunch_stats and the damper op reject bad arguments on the host."""
+    from pyheadtail_gb300 import _native as N
+    L = N.load(build_if_missing=False)
+    c = N.Coords()
+    for i, f in enumerate(('x', 'xp', 'y', 'yp', 'z', 'dp')):
+        setattr(c, f, 4096 * (i + 1))
+    c.n, c.dtype = 100, 0
+    st = N.Stats()
+    st.order, st.capacity, st.grid = 3, 1, 1
+    st.records, st.partials, st.ticket = 8192, 16384, 32768
+    assert L.phk_bunch_stats(ctypes.byref(c), None, ctypes.byref(st),
+                             None) == -4
+    st.order = 2
+    st.capacity = 0
+    assert L.phk_bunch_stats(ctypes.byref(c), None, ctypes.byref(st),
+                             None) == -2
+    st.capacity = 1
+    st.mask = 0x40
+    assert L.phk_bunch_stats(ctypes.byref(c), None, ctypes.byref(st),
+                             None) == -4
+    st.mask = 0
+    st.ticket = 0
+    assert L.phk_bunch_stats(ctypes.byref(c), None, ctypes.byref(st),
+                             None) == -1
+    st.ticket = 32768
+    st.means = 12
+    assert L.phk_bunch_stats(ctypes.byref(c), None, ctypes.byref(st),
+                             None) == -3
+    assert L.phk_bunch_stats_grid(-1, 0) == -2
+    prog = N.Program()
+    prog.n_ops = 1
+    prog.op[0].kind = N.OP_DAMPER
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(c), None, None,
+                       None) == -4           # no means pointer
+    assert 'damper' in N.last_error()
 
 
 @pytest.mark.parametrize('code', [0, 1])

@@ -51,5 +51,6 @@ def test_fixture_set_covers_every_stage():
                  'slicer_fixed', 'wake_resonator', 'wake_multiturn',
                  'wake_dynamic_cuts', 'wake_plates', 'c1_full', 'c2_full',
                  'bunch_statistics', 'wake_table_multiturn',
-                 'wake_table_lowbeta'):
+                 'wake_table_lowbeta', 'damper_resistive',
+                 'damper_reactive'):
         assert need in names
