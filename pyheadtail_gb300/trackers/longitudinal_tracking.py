@@ -273,8 +273,23 @@ class RFSystems(LongitudinalOneTurnMap):
     def track_transverse_shrinking(self, beam):
         self.track(beam)
 
+    @property
+    def Q_s(self):
+        """Small-amplitude synchrotron tune of this RF system at its
+        reference gamma: the formula of RFBucket.Q_s
+        (trackers/rf_bucket.py:268-279), which RFSystems.Q_s
+        (longitudinal_tracking.py:461-464) reads from its bucket."""
+        gamma = self.gamma
+        beta = np.sqrt(1 - gamma**-2)
+        p0 = np.sqrt(gamma**2 - 1) * self.mass * c
+        eta0 = self.alpha_array[0] - gamma**-2
+        hV = sum([h * self.voltages[i] for i, h in enumerate(self.harmonics)])
+        return np.sqrt(np.abs(self.charge) * np.abs(eta0) * hV /
+                       (2 * np.pi * p0 * beta * c))
+
     def get_bucket(self, *args, **kwargs):
-        raise NotImplementedError('RFBucket is host-side set-up of the '
+        raise NotImplementedError('RFBucket (separatrix, bucket-matched '
+                                  'distributions) is host-side set-up of the '
                                   'reference; build it with PyHEADTAIL')
 
 

@@ -217,3 +217,44 @@ CASES = {
                                     amplitude=[1e-11, 1e-11, -5e-12]),
                   rf(), wake(slicer(200), resonator())]),
 }
+
+
+# Synchrotron set-ups (machines/synchrotron.py): the machine's keyword
+# arguments (charge / mass: e / m_p, added by the builders), the bunch and
+# the extras of the turn loop.  Fixtures in synchrotron/<name>.npz.
+P0_26GEV = 26e9 * 1.602176634e-19 / 299792458.0
+SYNCHROTRON_CASES = {
+    # smooth optics in three segments, RF parameters -> the linear map's
+    # Q_s from the bucket formula, longitudinal map in the middle, a
+    # damper after each segment and a resonator wake at the end
+    'synchrotron_linear': dict(
+        machine=dict(optics_mode='smooth', circumference=C_SPS, n_segments=3,
+                     beta_x=54.6, beta_y=54.5, D_x=0.0, D_y=0.0,
+                     accQ_x=20.13, accQ_y=20.18, Qp_x=2.0, Qp_y=-1.0,
+                     app_x=3e-11, app_y=2e-11, app_xy=-1e-11,
+                     longitudinal_mode='linear', alpha_mom_compaction=ALPHA_C,
+                     h_RF=[4620], V_RF=[4.5e6], dphi_RF=[0.],
+                     p_increment=0., p0=P0_26GEV, RF_at='middle'),
+        bunch=dict(n=2000, seed=31, intensity=2.5e11, epsn_x=2e-6,
+                   epsn_y=2e-6, sigma_z=0.23),
+        damper_after_segments=(80., 120.),
+        wake=dict(n_slices=40, R=10e6, f=1e9, Q=1.),
+        n_turns=4),
+    # non-smooth optics, two-harmonic RF at the end of the ring; the bunch
+    # (cut at the separatrix by the reference) is handed over as data
+    'synchrotron_nonlinear': dict(
+        machine=dict(optics_mode='non-smooth',
+                     s=[0., 2000., 4500., C_SPS],
+                     alpha_x=[0.2, -0.8, 0.5, 0.2], beta_x=[50., 70., 30., 50.],
+                     D_x=[0., 0., 0., 0.], alpha_y=[-0.3, 0.6, -0.1, -0.3],
+                     beta_y=[45., 35., 60., 45.], D_y=[0., 0., 0., 0.],
+                     accQ_x=[0., 6.3, 13.9, 20.13],
+                     accQ_y=[0., 5.8, 12.7, 20.18], Qp_x=1.0, Qp_y=1.0,
+                     longitudinal_mode='non-linear',
+                     alpha_mom_compaction=ALPHA_C, h_RF=[4620, 4 * 4620],
+                     V_RF=[4.5e6, 0.45e6], dphi_RF=[0., np.pi],
+                     p_increment=0., p0=P0_26GEV, RF_at='end_of_transverse'),
+        bunch=dict(n=2000, seed=32, intensity=2.5e11, epsn_x=2e-6,
+                   epsn_y=2e-6, sigma_z=0.2),
+        damper_after_segments=None, wake=None, n_turns=3),
+}
