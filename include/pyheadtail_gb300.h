@@ -518,6 +518,36 @@ int phk_slice_noalloc(const phk_slicer *slicer, const phk_coords *coords,
                       int32_t *counts, double *mean_x, double *mean_y,
                       void *stream);
 
+/* ---- order statistics of z for UniformChargeSlicer
+ *      (particles/slicing.py:618-686): the reference argsorts z and cuts
+ *      the sorted bunch into equal-count slices; only the z values at the
+ *      slice-edge ranks are needed.  Three steps, all integer counting on
+ *      exact order keys (so the values are z_sorted[rank] bit for bit):
+ *  phk_charge_hist: hist[b] (uint32[K], zeroed by the caller) counts the
+ *    particles with tail <= z < head in bin b = clamp(int((z - tail) *
+ *    K / (head - tail)), 0, K-1); below[0] += #(z < tail), below[1] +=
+ *    #(z < head) (uint64[2], zeroed by the caller; NaN counts in neither).
+ *  phk_charge_gather: for particles inside the cuts whose bin b has
+ *    seg_of_bin[b] = s >= 0, their order keys go to keys[seg_off[s] ..
+ *    + seg_count[s]) in any order (fill: uint32[n_seg], zeroed).  A
+ *    segment that receives more than seg_count[s] keys sets
+ *    PHK_DEV_BAD_TABLE in *status and drops the extra keys.
+ *  phk_charge_select: out[t] = the tgt_rank[t]-th smallest value (0-based)
+ *    of segment tgt_seg[t].
+ * No counterpart of the split in the reference (it sorts the whole bunch). */
+int phk_charge_hist(const void *z, int64_t n, int32_t dtype, double tail,
+                    double head, int32_t K, uint32_t *hist, uint64_t *below,
+                    void *stream);
+int phk_charge_gather(const void *z, int64_t n, int32_t dtype, double tail,
+                      double head, int32_t K, const int32_t *seg_of_bin,
+                      const int64_t *seg_off, const int32_t *seg_count,
+                      uint32_t *fill, uint64_t *keys, int32_t *status,
+                      void *stream);
+int phk_charge_select(const uint64_t *keys, const int64_t *seg_off,
+                      const int32_t *seg_count, const int32_t *tgt_seg,
+                      const int32_t *tgt_rank, int32_t n_targets, double *out,
+                      int32_t *status, void *stream);
+
 /* CTAs of a phk_bunch_stats launch over n particles of dtype; sizes the
  * partials workspace (grid * PHK_STATS_LEN doubles). */
 int phk_bunch_stats_grid(int64_t n, int32_t dtype);

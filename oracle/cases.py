@@ -28,8 +28,9 @@ def table_path(name):
 
 def make_slicer(sp):
     z_cuts = None if sp['z_cuts'] is None else tuple(sp['z_cuts'])
-    return T.UniformBinSlicer(sp['n_slices'], n_sigma_z=sp['n_sigma_z'],
-                              z_cuts=z_cuts)
+    cls = (T.UniformChargeSlicer if sp.get('mode') == 'uniform_charge'
+           else T.UniformBinSlicer)
+    return cls(sp['n_slices'], n_sigma_z=sp['n_sigma_z'], z_cuts=z_cuts)
 
 
 def make_kicks(src, slicer):
@@ -125,6 +126,9 @@ def make_elements(spec, beam):
 
 def run(spec, beam, n_turns=None, record_turns=None):
     """Track ``beam`` through the case; return the fixture-shaped record."""
+    if 'random_seed' in spec:
+        import random
+        random.seed(spec['random_seed'])
     elements = make_elements(spec, beam)
     n_turns = spec['n_turns'] if n_turns is None else n_turns
     if record_turns is None:

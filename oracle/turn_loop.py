@@ -698,11 +698,16 @@ class UniformBinSlicer(object):
             head += abs(head) * 1e-15
         return tail, head
 
-    def slice(self, beam, statistics=()):
+    def bins_and_index(self, beam):
+        """compute_sliceset_kwargs, slicing.py:599-615."""
         tail, head = self.get_long_cuts(beam)
         width = (head - tail) / float(self.n_slices)
         z_bins = np.arange(tail, head + 1e-7 * width, width, dtype=np.float64)
         idx = np.floor((beam.z - tail) / width).astype(np.int32)
+        return z_bins, idx
+
+    def slice(self, beam, statistics=()):
+        z_bins, idx = self.bins_and_index(beam)
         ss = SliceSet(z_bins, idx, beam)
         for st in statistics:
             if st.startswith('mean_'):
@@ -730,6 +735,41 @@ class UniformBinSlicer(object):
 # --------------------------------------------------------------------------
 # Wakes: impedances/wakes.py, impedances/wake_kicks.py
 # --------------------------------------------------------------------------
+
+
+class UniformChargeSlicer(UniformBinSlicer):
+    """UniformChargeSlicer, particles/slicing.py:618-686: the bunch sorted
+    by z is cut into slices of equal particle count (the remainder of the
+    division goes to slices drawn with Python's random.sample); edges are
+    the midpoints between the last particle of a slice and the first of the
+    next; particles outside the cuts get index -1."""
+
+    mode = 'uniform_charge'
+
+    def bins_and_index(self, beam):
+        from random import sample
+        tail, head = self.get_long_cuts(beam)
+        S = self.n_slices
+        n = len(beam.z)
+        order = np.argsort(beam.z)
+        z_sorted = beam.z.take(order)
+        below_tail = np.searchsorted(z_sorted, tail)
+        from_head = n - np.searchsorted(z_sorted, head)
+        inside = n - below_tail - from_head
+        extra = sample(list(range(S)), inside % S)
+        per_slice = (inside // S) * np.ones(S, dtype=np.int32)
+        per_slice[extra] += 1
+        bounds = np.cumsum(np.hstack((below_tail, per_slice, from_head)),
+                           dtype=np.int32)[:-1]
+        z_bins = np.empty(S + 1)
+        z_bins[1:-1] = (z_sorted[bounds[1:-1] - 1] + z_sorted[bounds[1:-1]]) / 2
+        z_bins[0], z_bins[-1] = tail, head
+        idx_sorted = -np.ones(n, dtype=np.int32)
+        for k in range(S):
+            idx_sorted[bounds[k]:bounds[k + 1]] = k
+        idx = np.empty(n, dtype=np.int32)
+        np.put(idx, np.arange(n).take(order), idx_sorted)
+        return z_bins, idx
 
 
 def resonator_transverse(R_shunt, frequency, Q, yokoya):

@@ -117,13 +117,27 @@ def exact_edges(tail, width, n_slices, code):
     return _from_keys(khi, dt), neg
 
 
+def ceil_to_dtype(v, code):
+    """The smallest value of the coordinate dtype that is >= v."""
+    if code == _F64:
+        return np.float64(v)
+    f = np.float32(v)
+    if np.float64(f) < v:
+        f = np.nextafter(f, np.float32(np.inf))
+    return f
+
+
 class DeviceSlicer(object):
     """Exact bin tables of one (cuts, n_slices, dtype) on the device."""
 
-    def __init__(self, tail, head, n_slices, code, device):
+    def __init__(self, tail, head, n_slices, code, device, edges=None):
         tail = float(tail)
         width = (head - tail) / float(n_slices)
-        e, neg = exact_edges(tail, width, n_slices, code)
+        if edges is None:
+            e, neg = exact_edges(tail, width, n_slices, code)
+        else:
+            # given lower edges (non-uniform slices), ascending in z
+            e, neg = np.ascontiguousarray(edges, dtype=np_dtype(code)), False
         self.tail, self.head, self.width = tail, head, width
         self.n_slices = n_slices
         self.code = code

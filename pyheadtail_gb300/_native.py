@@ -186,6 +186,17 @@ SIGNATURES = {
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_void_p],
     'phk_bunch_stats_grid': [ctypes.c_int64, ctypes.c_int32],
+    'phk_charge_hist': [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                        ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    'phk_charge_gather': [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                          ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_void_p],
+    'phk_charge_select': [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
     'phk_bunch_stats': [ctypes.POINTER(Coords), ctypes.POINTER(KickSet),
                         ctypes.POINTER(Stats), ctypes.c_void_p],
 }

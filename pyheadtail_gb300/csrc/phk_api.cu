@@ -468,6 +468,67 @@ int phk_wake_tc_run(const phk_wake_tc* w, void* stream) {
     return launch_wake_tc(w, (cudaStream_t)stream);
 }
 
+static int check_charge_range(const void* z, int64_t n, int32_t dtype,
+                              double tail, double head, int32_t K,
+                              const char* who) {
+    int r = check_dtype(dtype, who);
+    if (r) return r;
+    if (n < 0) return set_error(PHK_ESIZE, "%s: n < 0", who);
+    if (n > 0 && !z) return set_error(PHK_ENULL, "%s: z is NULL", who);
+    if (reinterpret_cast<uintptr_t>(z) % dsize(dtype))
+        return set_error(PHK_EALIGN, "%s: z misaligned", who);
+    if (!(head > tail))
+        return set_error(PHK_EPARAM, "%s: head %g <= tail %g", who, head, tail);
+    if (K < 1 || K > (1 << 24))
+        return set_error(PHK_ESIZE, "%s: K %d outside [1, 2^24]", who, K);
+    return PHK_OK;
+}
+
+int phk_charge_hist(const void* z, int64_t n, int32_t dtype, double tail,
+                    double head, int32_t K, uint32_t* hist, uint64_t* below,
+                    void* stream) {
+    const char* who = "phk_charge_hist";
+    int r = check_charge_range(z, n, dtype, tail, head, K, who);
+    if (r) return r;
+    if (!hist || !below)
+        return set_error(PHK_ENULL, "%s: hist / below is NULL", who);
+    if (n == 0) return PHK_OK;
+    return launch_charge_hist(z, n, dtype, tail, head, K, hist,
+                              reinterpret_cast<unsigned long long*>(below),
+                              (cudaStream_t)stream);
+}
+
+int phk_charge_gather(const void* z, int64_t n, int32_t dtype, double tail,
+                      double head, int32_t K, const int32_t* seg_of_bin,
+                      const int64_t* seg_off, const int32_t* seg_count,
+                      uint32_t* fill, uint64_t* keys, int32_t* status,
+                      void* stream) {
+    const char* who = "phk_charge_gather";
+    int r = check_charge_range(z, n, dtype, tail, head, K, who);
+    if (r) return r;
+    if (!seg_of_bin || !seg_off || !seg_count || !fill || !keys)
+        return set_error(PHK_ENULL, "%s: a table is NULL", who);
+    if (n == 0) return PHK_OK;
+    return launch_charge_gather(z, n, dtype, tail, head, K, seg_of_bin,
+                                seg_off, seg_count, fill,
+                                reinterpret_cast<unsigned long long*>(keys),
+                                status, (cudaStream_t)stream);
+}
+
+int phk_charge_select(const uint64_t* keys, const int64_t* seg_off,
+                      const int32_t* seg_count, const int32_t* tgt_seg,
+                      const int32_t* tgt_rank, int32_t n_targets, double* out,
+                      int32_t* status, void* stream) {
+    const char* who = "phk_charge_select";
+    if (n_targets < 0) return set_error(PHK_ESIZE, "%s: n_targets < 0", who);
+    if (n_targets == 0) return PHK_OK;
+    if (!keys || !seg_off || !seg_count || !tgt_seg || !tgt_rank || !out)
+        return set_error(PHK_ENULL, "%s: a table is NULL", who);
+    return launch_charge_select(
+        reinterpret_cast<const unsigned long long*>(keys), seg_off, seg_count,
+        tgt_seg, tgt_rank, n_targets, out, status, (cudaStream_t)stream);
+}
+
 int phk_bunch_stats_grid(int64_t n, int32_t dtype) {
     int r = check_dtype(dtype, "phk_bunch_stats_grid");
     if (r) return r;

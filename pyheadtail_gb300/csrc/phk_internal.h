@@ -59,6 +59,20 @@ int launch_batch_finalize(const phk_accum* acc, int nb, const int32_t* bcols,
 int launch_wake_batch(const phk_wake_set* sets, int nb, int n_slices,
                       int n_kicks, cudaStream_t stream);
 int stats_grid(int64_t n, int32_t dtype);
+int launch_charge_hist(const void* z, int64_t n, int32_t dtype, double tail,
+                       double head, int32_t K, uint32_t* hist,
+                       unsigned long long* below, cudaStream_t stream);
+int launch_charge_gather(const void* z, int64_t n, int32_t dtype,
+                         double tail, double head, int32_t K,
+                         const int32_t* seg_of_bin, const int64_t* seg_off,
+                         const int32_t* seg_count, uint32_t* fill,
+                         unsigned long long* keys, int32_t* status,
+                         cudaStream_t stream);
+int launch_charge_select(const unsigned long long* keys,
+                         const int64_t* seg_off, const int32_t* seg_count,
+                         const int32_t* tgt_seg, const int32_t* tgt_rank,
+                         int32_t n_targets, double* out, int32_t* status,
+                         cudaStream_t stream);
 int launch_stats(const phk_coords* c, const phk_kick_set* pk,
                  const phk_stats* s, cudaStream_t stream);
 

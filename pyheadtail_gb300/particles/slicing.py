@@ -96,7 +96,13 @@ class SliceSet(Printing):
                     'slice_index_of_particle of a SliceSet must be read '
                     'before the beam is tracked further (the GPU SliceSet '
                     'keeps no copy of z); request it right after slicing')
-            self._slice_index_of_particle = _index_pass(b, self._dslicer)
+            idx = _index_pass(b, self._dslicer)
+            if self.mode == 'uniform_charge':
+                # the reference marks particles outside the cuts with -1
+                # (slicing.py:668-673)
+                idx = torch.where((idx >= 0) & (idx < self.n_slices), idx,
+                                  torch.full_like(idx, -1))
+            self._slice_index_of_particle = idx
         return self._slice_index_of_particle
 
     @property
@@ -290,12 +296,167 @@ class UniformBinSlicer(Slicer):
         add_statistics(sliceset, beam, statistics)
 
 
+def charge_bins_for(n):
+    """Coarse bins of the order-statistics histogram: about 64 particles per
+    bin, 256 to 8192 bins."""
+    return int(min(8192, max(256, 1 << int(np.ceil(np.log2(max(n, 2) / 64.))))))
+
+
+def charge_ranks(n, n_cut_tail, n_cut_head, n_slices):
+    """Particles per slice and the ranks (inside the cuts) of the order
+    statistics a uniform-charge slicing needs (slicing.py:645-665):
+    z_sorted[first - 1] and z_sorted[first] for the first particle of every
+    slice but the first.  Draws the reference's random.sample."""
+    from random import sample
+    S = n_slices
+    n_part_within_cuts = n - n_cut_tail - n_cut_head
+    rand_slice_i = sample(list(range(S)), n_part_within_cuts % S)
+    n_part_per_slice = (n_part_within_cuts // S) * np.ones(S, dtype=np.int32)
+    n_part_per_slice[rand_slice_i] += 1
+    if n_part_within_cuts < S:
+        raise ValueError('UniformChargeSlicer: %d particles inside the cuts '
+                         'for %d slices' % (n_part_within_cuts, S))
+    n_all = np.hstack((n_cut_tail, n_part_per_slice, n_cut_head))
+    first_indices = np.cumsum(n_all, dtype=np.int64)[:-1]
+    f = first_indices[1:-1] - n_cut_tail
+    return n_part_per_slice, np.concatenate([f - 1, f])
+
+
+def charge_segments(hist, ranks):
+    """Tables of phk_charge_gather / _select: the coarse bin holding each
+    rank becomes a segment; every rank's segment and rank inside it."""
+    h = np.asarray(hist, dtype=np.int64)
+    cum = np.cumsum(h)
+    start = cum - h
+    tb = np.searchsorted(cum, ranks, side='right')
+    ub, inv = np.unique(tb, return_inverse=True)
+    seg_count = h[ub]
+    seg_of_bin = -np.ones(len(h), dtype=np.int32)
+    seg_of_bin[ub] = np.arange(len(ub), dtype=np.int32)
+    return dict(seg_of_bin=seg_of_bin, seg_count=seg_count,
+                seg_off=np.concatenate([[0], np.cumsum(seg_count)[:-1]]),
+                tgt_seg=inv, tgt_rank=np.asarray(ranks) - start[tb])
+
+
+def charge_bins_and_edges(vals, tail, head, n_slices, code):
+    """z_bins of the reference (slicing.py:661-665: midpoints between the
+    last particle of a slice and the first of the next) and the lower edges
+    the device bins on: the first particle of every slice, the cuts rounded
+    up to the coordinate dtype at both ends."""
+    S = n_slices
+    lo, hi = vals[:S - 1], vals[S - 1:]
+    z_bins = np.empty(S + 1)
+    z_bins[1:-1] = (lo + hi) / 2
+    z_bins[0], z_bins[-1] = tail, head
+    edges = np.empty(S + 1, dtype=E.np_dtype(code))
+    edges[0] = E.ceil_to_dtype(tail, code)
+    edges[1:S] = hi
+    edges[S] = E.ceil_to_dtype(head, code)
+    return z_bins, edges
+
+
+class UniformChargeSlicer(Slicer):
+    """Slices of equal particle count over the cuts (slicing.py:618-686).
+
+    The reference argsorts z; here the slice edges are the order statistics
+    of z at the reference's ranks, found on the device without a sort
+    (phk_charge_hist / _gather / _select), and the particles are then
+    binned on those edges like a uniform-bin slicing.  The number of
+    particles per slice follows the reference exactly, including its
+    ``random.sample`` of the slices that receive one extra particle
+    (Python's ``random`` module, consumed the same way).  Slice indices,
+    z_bins and counts are the reference's unless two particles share a z
+    value at a slice edge (the reference's assignment then depends on its
+    sort's order of equal keys)."""
+
+    def __init__(self, n_slices, n_sigma_z=None, z_cuts=None, *args,
+                 **kwargs):
+        if n_sigma_z and z_cuts:
+            raise ValueError('Both arguments n_sigma_z and z_cuts are given '
+                             'while only one is accepted!')
+        if not 1 <= n_slices <= N.PHK_MAX_SLICES:
+            raise ValueError('n_slices must be in [1, %d]' % N.PHK_MAX_SLICES)
+        self.config = ('uniform_charge', n_slices, n_sigma_z, z_cuts)
+
+    def times(self, z_bins, beta):
+        zc = z_bins[:-1] + 0.5 * (z_bins[1:] - z_bins[:-1])
+        return zc / (beta * c)
+
+    def charge_edges(self, beam, tail, head):
+        """compute_sliceset_kwargs (slicing.py:636-686) on the device:
+        returns the DeviceSlicer of this slicing and its z_bins."""
+        n, S = beam.macroparticlenumber, self.n_slices
+        dev, code = beam._device, beam._code
+        z = beam._c['z']
+        stream = E.stream_handle()
+        K = charge_bins_for(n)
+        hist = torch.zeros(K, dtype=torch.int32, device=dev)
+        below = torch.zeros(2, dtype=torch.int64, device=dev)
+        N.call('phk_charge_hist', z.data_ptr(), n, code, float(tail),
+               float(head), K, hist.data_ptr(), below.data_ptr(), stream)
+        h = hist.cpu().numpy().astype(np.int64)
+        b = below.cpu().numpy()
+        n_cut_tail, n_cut_head = int(b[0]), n - int(b[1])
+        per_slice, ranks = charge_ranks(n, n_cut_tail, n_cut_head, S)
+        vals = np.empty(0)
+        if len(ranks):
+            tab = charge_segments(h, ranks)
+            t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(
+                a, dtype=dt)).to(dev)
+            d_sob = t(tab['seg_of_bin'], np.int32)
+            d_off = t(tab['seg_off'], np.int64)
+            d_cnt = t(tab['seg_count'], np.int32)
+            d_tseg = t(tab['tgt_seg'], np.int32)
+            d_trank = t(tab['tgt_rank'], np.int32)
+            keys = torch.empty(max(1, int(tab['seg_count'].sum())),
+                               dtype=torch.int64, device=dev)
+            fill = torch.zeros(len(tab['seg_count']), dtype=torch.int32,
+                               device=dev)
+            status = torch.zeros(1, dtype=torch.int32, device=dev)
+            out = torch.empty(len(ranks), dtype=torch.float64, device=dev)
+            N.call('phk_charge_gather', z.data_ptr(), n, code, float(tail),
+                   float(head), K, d_sob.data_ptr(), d_off.data_ptr(),
+                   d_cnt.data_ptr(), fill.data_ptr(), keys.data_ptr(),
+                   status.data_ptr(), stream)
+            N.call('phk_charge_select', keys.data_ptr(), d_off.data_ptr(),
+                   d_cnt.data_ptr(), d_tseg.data_ptr(), d_trank.data_ptr(),
+                   len(ranks), out.data_ptr(), status.data_ptr(), stream)
+            vals = out.cpu().numpy()
+            if int(status.item()):
+                raise N.PhkError('UniformChargeSlicer: inconsistent order '
+                                 'statistics tables (device status %d)'
+                                 % int(status.item()))
+        z_bins, edges = charge_bins_and_edges(vals, tail, head, S, code)
+        ds = E.DeviceSlicer(tail, head, S, code, dev, edges=edges)
+        ds.n_part_per_slice = per_slice
+        return ds, z_bins
+
+    def slice(self, beam, *args, **kwargs):
+        """Slicer.slice (slicing.py:348-381) on the GPU."""
+        stats = kwargs.get('statistics', None)
+        ss = make_slice_set(self, beam, with_means=bool(stats))
+        if stats:
+            add_statistics(ss, beam, stats)
+        return ss
+
+    def add_statistics(self, sliceset, beam, statistics):
+        add_statistics(sliceset, beam, statistics)
+
+
 def make_slice_set(slicer, beam, with_means=False, moments_out=None):
     """Flush the beam's pending program with a fused slicing pass and wrap
     the per-slice results in a SliceSet."""
     tail, head = slicer.get_long_cuts(beam)
-    ds = slicer.device_slicer(tail, head, beam)
     eng = beam._engine
+    if slicer.mode == 'uniform_charge':
+        # the edges follow from the z the pending program produces: run it
+        # first (pending kicks do not move z and stay pending)
+        if eng.ops:
+            eng.flush()
+        ds, z_bins = slicer.charge_edges(beam, tail, head)
+    else:
+        ds = slicer.device_slicer(tail, head, beam)
+        z_bins = slicer.z_bins(tail, head)
     part, grid = eng.workspace(slicer.n_slices)
     acc = E.AccumRequest(ds, part, grid)
     eng.flush(acc)
@@ -314,7 +475,7 @@ def make_slice_set(slicer, beam, with_means=False, moments_out=None):
            E.stream_handle())
     params = Slicer.extract_beam_parameters(beam)
     params['is_sorted'] = False
-    ss = SliceSet(slicer.z_bins(tail, head), slicer.mode, ds, beam, counts,
+    ss = SliceSet(z_bins, slicer.mode, ds, beam, counts,
                   beam_parameters=params)
     if mx is not None:
         ss.mean_x = mx

@@ -52,10 +52,10 @@ def linear_map(Q_s=0.017, alpha=ALPHA_C, D_x=0., D_y=0.):
     return dict(type='linear_map', Q_s=Q_s, alpha=[alpha], D_x=D_x, D_y=D_y)
 
 
-def slicer(n_slices, z_cuts=Z_CUTS, n_sigma_z=None):
+def slicer(n_slices, z_cuts=Z_CUTS, n_sigma_z=None, mode='uniform_bin'):
     return dict(n_slices=n_slices,
                 z_cuts=None if z_cuts is None else list(z_cuts),
-                n_sigma_z=n_sigma_z)
+                n_sigma_z=n_sigma_z, mode=mode)
 
 
 def resonator(R=10e6, f=1e9, Q=1., n_turns_wake=1, kind='circular'):
@@ -207,6 +207,22 @@ CASES = {
         elements=[damper(25., 0., phase=60., local_beta=50.),
                   smooth_transverse(), linear_map(),
                   wake(slicer(40), resonator())]),
+    # UniformChargeSlicer: equal-count slices (Python's random module picks
+    # the slices with one extra particle), the dot-product wake; fixed
+    # cuts, and cuts from the bunch (n_sigma_z) with a resistive wall
+    'charge_slicer': dict(
+        beam=beam_params(1203, 28), n_turns=1, random_seed=5,
+        elements=[probe(slicer(37, mode='uniform_charge'),
+                        ['mean_x', 'mean_y', 'sigma_z', 'epsn_x']),
+                  probe(slicer(16, z_cuts=(-0.2, 0.35),
+                               mode='uniform_charge'))]),
+    'wake_charge_slicer': dict(
+        beam=beam_params(1200, 29), n_turns=4, random_seed=6,
+        elements=[smooth_transverse(chroma=[-0.6, -0.6]), rf(),
+                  wake(slicer(50, z_cuts=None, n_sigma_z=3,
+                              mode='uniform_charge'),
+                       resonator(),
+                       resistive_wall(n_turns_wake=1))]),
     'c1_full': dict(
         beam=beam_params(1000, 0), n_turns=5,
         elements=[smooth_transverse(), linear_map(),

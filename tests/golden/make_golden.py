@@ -41,6 +41,26 @@ def build_reference(ref, scratch):
     sys.path.insert(0, scratch)
 
 
+def patch_reference_numpy2():
+    """PyHEADTAIL v1.16.5's UniformChargeSlicer computes its per-slice
+    counts as (numpy int64 scalar) * (int32 array), which NumPy 2 promotes
+    to int64 (NEP 50); its Cython statistics then reject the buffer
+    ("expected 'int' but got 'long'").  Cast the counts back to the int32
+    the code intends; every value is unchanged."""
+    from PyHEADTAIL.particles import slicing
+    orig = slicing.UniformChargeSlicer.compute_sliceset_kwargs
+    if getattr(orig, '_int32_counts', False):
+        return
+
+    def compute_sliceset_kwargs(self, beam):
+        kw = orig(self, beam)
+        kw['n_macroparticles_per_slice'] = np.asarray(
+            kw['n_macroparticles_per_slice'], dtype=np.int32)
+        return kw
+    compute_sliceset_kwargs._int32_counts = True
+    slicing.UniformChargeSlicer.compute_sliceset_kwargs = compute_sliceset_kwargs
+
+
 def make_beam(bp):
     from scipy.constants import m_p, e
     from PyHEADTAIL.particles import generators
@@ -59,9 +79,14 @@ def make_beam(bp):
 
 
 def make_slicer(sp):
-    from PyHEADTAIL.particles.slicing import UniformBinSlicer
+    from PyHEADTAIL.particles.slicing import (UniformBinSlicer,
+                                              UniformChargeSlicer)
     from PyHEADTAIL.general.printers import SilentPrinter
     z_cuts = None if sp['z_cuts'] is None else tuple(sp['z_cuts'])
+    if sp.get('mode') == 'uniform_charge':
+        return UniformChargeSlicer(sp['n_slices'], n_sigma_z=sp['n_sigma_z'],
+                                   z_cuts=z_cuts,
+                                   warningprinter=SilentPrinter())
     return UniformBinSlicer(sp['n_slices'], n_sigma_z=sp['n_sigma_z'],
                             z_cuts=z_cuts, warningprinter=SilentPrinter())
 
@@ -157,6 +182,9 @@ COORDS = ('x', 'xp', 'y', 'yp', 'z', 'dp')
 def run_case(name, spec):
     beam = make_beam(spec['beam'])
     rec = {'spec': json.dumps(spec)}
+    if 'random_seed' in spec:
+        import random
+        random.seed(spec['random_seed'])
     for k in COORDS:
         rec['init_' + k] = getattr(beam, k).copy()
     elements = make_elements(spec, beam)
@@ -203,6 +231,7 @@ def main():
     a = ap.parse_args()
     build_reference(a.ref, a.scratch)
     import PyHEADTAIL  # noqa: F401
+    patch_reference_numpy2()
     for name in (a.cases or sorted(C.CASES)):
         run_case(name, C.CASES[name])
         print('wrote', name)

@@ -23,6 +23,10 @@ def make_beam(bp, coords, precision='fp64'):
 
 def make_slicer(sp):
     z_cuts = None if sp['z_cuts'] is None else tuple(sp['z_cuts'])
+    if sp.get('mode') == 'uniform_charge':
+        from pyheadtail_gb300.particles.slicing import UniformChargeSlicer
+        return UniformChargeSlicer(sp['n_slices'], n_sigma_z=sp['n_sigma_z'],
+                                   z_cuts=z_cuts, warningprinter=SP)
     return UniformBinSlicer(sp['n_slices'], n_sigma_z=sp['n_sigma_z'],
                             z_cuts=z_cuts, warningprinter=SP)
 
@@ -101,6 +105,9 @@ def _np(t):
 
 
 def run(spec, beam, n_turns=None, record_turns=None):
+    if 'random_seed' in spec:
+        import random
+        random.seed(spec['random_seed'])
     elements = make_elements(spec, beam)
     n_turns = spec['n_turns'] if n_turns is None else n_turns
     if record_turns is None:

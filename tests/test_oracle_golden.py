@@ -52,5 +52,5 @@ def test_fixture_set_covers_every_stage():
                  'wake_dynamic_cuts', 'wake_plates', 'c1_full', 'c2_full',
                  'bunch_statistics', 'wake_table_multiturn',
                  'wake_table_lowbeta', 'damper_resistive',
-                 'damper_reactive'):
+                 'damper_reactive', 'charge_slicer', 'wake_charge_slicer'):
         assert need in names
