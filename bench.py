@@ -738,6 +738,67 @@ def run_reference_c4(a, rank, world):
     }))
 
 
+# ------------------------------------------------------------ statistics pass
+
+def run_stats_pass(a, rank, world):
+    """Time the bunch statistics pass (Particles.launch_stats ->
+    phk_bunch_stats) on the workload's bunch size with random coordinates
+    made on the device: centroids of x and y (order 1), centroids of all
+    six coordinates, and the order-2 pass behind sigma / emittance / Twiss.
+    Prints one JSON line; not the headline metric."""
+    import torch
+    from pyheadtail_gb300.particles.particles import Particles
+    from scipy.constants import e, m_p
+    if rank != 0:
+        return
+    w = WORKLOADS[a.workload]
+    n = w['n']
+    peak, peak_kind = measured_peaks()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32,
+                        device='cuda')
+    cases = {}
+    for prec in ('fp32', 'fp64'):
+        if a.form not in ('all', prec):
+            continue
+        dt = torch.float32 if prec == 'fp32' else torch.float64
+        g = torch.Generator(device='cuda').manual_seed(w['seed'])
+        coords = {q: 1e-3 * torch.randn(n, dtype=dt, device='cuda',
+                                        generator=g)
+                  for q in ('x', 'xp', 'y', 'yp', 'z', 'dp')}
+        beam = Particles(n, 1., e, m_p, C_RING, GAMMA,
+                         coords_n_momenta_dict=coords, precision=prec)
+        del coords
+        rec = torch.empty(34, dtype=torch.float64, device='cuda')
+        for label, order, mask, nq in (('centroids x y', 1, 0x5, 2),
+                                       ('centroids, six', 1, 0x3f, 6),
+                                       ('order 2', 2, 0x3f, 6)):
+            ms = []
+            for it in range(a.warmup + a.steps):
+                flush_l2(flush)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                beam.launch_stats(rec, order=order, mask=mask)
+                e1.record()
+                torch.cuda.synchronize()
+                if it >= a.warmup:
+                    ms.append(e0.elapsed_time(e1))
+            t = float(np.median(ms))
+            gbs = n * nq * beam.x.element_size() / (t * 1e-3) / 1e9
+            cases['%s %s' % (prec, label)] = {
+                'ms': t, 'particles_per_s': n / (t * 1e-3), 'GB/s': gbs,
+                'frac_of_hbm': gbs / peak, 'peak_kind': peak_kind}
+        del beam
+        torch.cuda.empty_cache()
+    head = cases.get('fp32 centroids, six') or next(iter(cases.values()))
+    print(json.dumps({
+        'metric': 'bunch statistics pass: particles/s', 'value':
+        head['particles_per_s'], 'unit': 'particles/s', 'n_gpus': 1,
+        'steps': a.steps, 'warmup': a.warmup,
+        'config': {'n_macroparticles': n, 'l2': 'flushed between passes'},
+        'cases': cases}))
+
+
 # ------------------------------------------------------------ reference arm
 
 def run_reference(a, rank, world):
@@ -789,12 +850,16 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-autotune', dest='autotune', action='store_false',
                     help='batched workload: skip timing the launch shapes')
+    ap.add_argument('--stats-pass', action='store_true',
+                    help='time the bunch statistics pass instead of the turn')
     a = ap.parse_args()
     a.steps_given = any(x == '--steps' or x.startswith('--steps=')
                         for x in sys.argv[1:])
     a.warmup = max(3, a.warmup)
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
+    if a.stats_pass and a.impl == 'ours':
+        return run_stats_pass(a, rank, world)
     if a.impl == 'reference':
         if a.workload == 'c4':
             return run_reference_c4(a, rank, world)
