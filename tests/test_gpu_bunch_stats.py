@@ -264,3 +264,40 @@ def test_bunch_monitor_on_gpu(lib, tmp_path):
         pytest.skip('h5py output')
     for s in stats:
         np.testing.assert_allclose(out[s], direct[s], rtol=1e-14, err_msg=s)
+
+
+def test_slice_and_particle_monitors_on_gpu(lib, tmp_path):
+    """SliceMonitor and ParticleMonitor on a GPU bunch after a wake turn:
+    the file holds what the slice set and the bunch report directly."""
+    import os
+    import cases as C
+    import gpu_cases as G
+    from oracle import cases as OC
+    from pyheadtail_gb300.monitors.monitors import (ParticleMonitor,
+                                                    SliceMonitor)
+    spec = dict(C.CASES['wake_resonator'])
+    spec['beam'] = C.beam_params(30000, 19)
+    beam = G.make_beam(spec['beam'], OC.make_beam(spec['beam']).coords())
+    els = G.make_elements(spec, beam)
+    sl = G.make_slicer(C.slicer(20))
+    fn = str(tmp_path / 'sm')
+    sm = SliceMonitor(fn, 3, sl, write_buffer_every=2, buffer_size=2)
+    pm = ParticleMonitor(str(tmp_path / 'pm'), stride=7)
+    counts, mean_x = [], []
+    for _ in range(3):
+        for _, el in els:
+            el.track(beam)
+        sm.dump(beam)
+        pm.dump(beam)
+        ss = beam.get_slices(sl, statistics=True)
+        counts.append(ss.n_macroparticles_per_slice.cpu().numpy())
+        mean_x.append(beam.mean_x())
+    if not os.path.exists(fn + '.npz'):
+        pytest.skip('h5py output')
+    with np.load(fn + '.npz') as f:
+        np.testing.assert_array_equal(f['Slices/n_macroparticles_per_slice'],
+                                      np.array(counts).T)
+        np.testing.assert_allclose(f['Bunch/mean_x'], mean_x, rtol=0,
+                                   atol=1e-12 * beam.sigma_x())
+    with np.load(str(tmp_path / 'pm') + '.Step#2.npz') as f:
+        np.testing.assert_array_equal(f['x'], beam.x.cpu().numpy()[::7])

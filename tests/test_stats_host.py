@@ -6,7 +6,9 @@
   fixture's coordinates, for all 26 statistics of Particles.
 * Edge cases of the formulas: n = 0, 1, 2, constant dp.
 * BunchMonitor's ring / cursor / write logic, driven by a CPU stand-in
-  bunch that writes the record phk_bunch_stats would write.
+  bunch that writes the record phk_bunch_stats would write; SliceMonitor's
+  device buffers and file layout, and ParticleMonitor's strided dumps, with
+  CPU stand-ins of the bunch and its slice set.
 """
 import json
 import os
@@ -155,3 +157,73 @@ def test_bunch_monitor_ring_and_writes(tmp_path):
         mon.dump(b)
     with pytest.raises(ValueError):
         BunchMonitor(fn, 4, write_buffer_every=8, buffer_size=4)
+
+
+class _HostSliceSet(object):
+    def __init__(self, c, n_slices):
+        z = c['z']
+        edges = np.linspace(-1., 1., n_slices + 1)
+        idx = np.searchsorted(edges, z, side='right') - 1
+        inside = (idx >= 0) & (idx < n_slices)
+        self.n_macroparticles_per_slice = torch.from_numpy(
+            np.bincount(idx[inside], minlength=n_slices).astype(np.int32))
+        for st in ('mean_x', 'mean_xp', 'mean_y', 'mean_yp', 'mean_z',
+                   'mean_dp', 'sigma_x', 'sigma_y', 'sigma_z', 'sigma_dp',
+                   'epsn_x', 'epsn_y', 'epsn_z'):
+            setattr(self, st, torch.from_numpy(
+                np.arange(n_slices, dtype=np.float64) * (1 + len(st)) +
+                float(np.sum(z))))
+
+
+class _HostSlicedBunch(_HostBunch):
+    def get_slices(self, slicer, statistics=None):
+        return _HostSliceSet(self.c, slicer.n_slices)
+
+
+class _Slicer(object):
+    n_slices = 7
+
+
+def test_slice_monitor_writes(tmp_path):
+    from pyheadtail_gb300.monitors.monitors import SliceMonitor
+    rng = np.random.RandomState(2)
+    fn = str(tmp_path / 'sm')
+    n_steps = 9
+    mon = SliceMonitor(fn, n_steps, _Slicer(), {'a': 1},
+                       write_buffer_every=4, buffer_size=4)
+    want_b, want_s = [], []
+    for step in range(n_steps):
+        c = {q: rng.normal(size=300) * 0.3 for q in COORDS}
+        b = _HostSlicedBunch(c)
+        mon.dump(b)
+        want_b.append(np.mean(c['x']))
+        want_s.append(_HostSliceSet(c, 7).n_macroparticles_per_slice.numpy())
+    if os.path.exists(fn + '.h5'):
+        pytest.skip('h5py present')
+    with np.load(fn + '.npz') as f:
+        np.testing.assert_allclose(f['Bunch/mean_x'], want_b, rtol=1e-12)
+        np.testing.assert_array_equal(
+            f['Slices/n_macroparticles_per_slice'], np.array(want_s).T)
+        assert f['Slices/mean_x'].shape == (7, n_steps)
+
+
+class _ParticleBunch(object):
+    def __init__(self, n):
+        for q in COORDS:
+            setattr(self, q, torch.arange(n, dtype=torch.float64) * (1 + len(q)))
+        self.id = torch.arange(1, n + 1, dtype=torch.int32)
+
+
+def test_particle_monitor_writes(tmp_path):
+    from pyheadtail_gb300.monitors.monitors import ParticleMonitor
+    fn = str(tmp_path / 'pm')
+    mon = ParticleMonitor(fn, stride=3)
+    b = _ParticleBunch(20)
+    mon.dump(b)
+    mon.dump(b, arrays_dict={'extra': np.arange(20)})
+    if os.path.exists(fn + '.h5part'):
+        pytest.skip('h5py present')
+    with np.load(fn + '.Step#1.npz') as f:
+        np.testing.assert_array_equal(f['id'], np.arange(1, 21)[::3])
+        np.testing.assert_array_equal(f['x'], np.arange(20)[::3] * 2.)
+        np.testing.assert_array_equal(f['extra'], np.arange(20)[::3])
