@@ -42,7 +42,7 @@ extern "C" {
 
 /* coordinate storage types */
 #define PHK_F64 0 /* plain form: FP64 coordinates, FP64 arithmetic          */
-#define PHK_F32 1 /* precision form: FP32 coordinates, see DESIGN notes     */
+#define PHK_F32 1 /* precision form: FP32 coordinates, float-float phases */
 
 /* limits of the parameter blocks */
 #define PHK_MAX_OPS 12
