@@ -11,10 +11,12 @@ A step is one turn: [TransverseSegmentMap, RFSystems, WakeField].
 
 ``value``  plain FP64 form (the drop-in), device time of the turn replayed as
            a CUDA graph, inputs resident, L2 flushed between steps.
-``e2e``    the same turn(s) through the public API, wall clock: the step's
-           coordinates copied from pinned host memory into the beam's arrays,
-           one replay of the captured turn (``TurnGraph.replay``), the bunch
-           centroid read back (``beam.mean_x()``, ``beam.mean_y()``).
+``e2e``    the same turn(s) through the public API, wall clock: every step
+           a bunch's coordinates copied from pinned host memory into a beam's
+           arrays, one replay of its captured turn(s), its centroid record
+           (order-1 statistics of x and y) copied back
+           (``turngraph.StreamedTurns``: two beams take the steps in turn, so
+           one step's copy overlaps the previous step's turn).
 ``forms``  the FP32 precision form measured the same way.
 ``--impl reference`` times the CPU oracle (a NumPy restatement of the
 reference's turn loop, bit-identical to it on the golden fixtures) on a
@@ -288,7 +290,7 @@ def time_form(w, coords, precision, steps, warmup, flush):
     """Device time per turn (graph replay), track-kernel time, e2e."""
     import torch
     from pyheadtail_gb300 import _native as N
-    from pyheadtail_gb300.turngraph import TurnGraph
+    from pyheadtail_gb300.turngraph import StreamedTurns, TurnGraph
     beam, elements = build_gpu(w, coords, precision)
     ring = max(1, w['rw_turns'])
     warm = max(warmup, ring + 2, 3)
@@ -330,26 +332,33 @@ def time_form(w, coords, precision, steps, warmup, flush):
     evs = beam._engine.track_events
     beam._engine.track_events = None
     track_ms = [a.elapsed_time(b) for a, b in evs]
-    # e2e: public API, every step the bunch from pinned host memory into
-    # the beam's coordinate arrays, one replay of the captured turn(s),
-    # the centroid read back
+    # e2e: public API (turngraph.StreamedTurns), every step a bunch from
+    # pinned host memory into a beam's coordinate arrays, one replay of its
+    # captured turn(s), its centroid record read back; two beams take the
+    # steps in turn, so a step's copy overlaps the previous step's turn
     host = {k: torch.from_numpy(np.ascontiguousarray(
         v.astype(np.float64 if precision == 'fp64' else np.float32))
     ).pin_memory() for k, v in coords.items()}
     h2d = sum(t.numel() * t.element_size() for t in host.values())
-    e2e_s = []
-    for i in range(max(3, steps // 2) + 1):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for k, t in host.items():
-            getattr(beam, k).copy_(t, non_blocking=True)
-        tg.replay(1)
-        cx, cy = beam.mean_x(), beam.mean_y()
-        if i:                            # the first step loads torch's kernels
-            e2e_s.append(time.perf_counter() - t0)
+    del tg, beam, elements
+    torch.cuda.empty_cache()
+    st = StreamedTurns(lambda k: build_gpu(w, coords, precision), n_slots=2,
+                       warmup_turns=warm)
+    for _ in range(4):                   # loads torch's copy / event paths
+        st.push(host)
+    st.drain()
+    n_e2e = max(4, steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(n_e2e):
+        st.push(host)
+    cx, cy = st.drain()[-1]
+    e2e_s = [(time.perf_counter() - t0) / n_e2e] * n_e2e
+    del st
+    torch.cuda.empty_cache()
     return dict(graph_ms=graph_ms, turns_per_step=tpg, track_ms=track_ms,
-                e2e_s=e2e_s, h2d=h2d, d2h=16, kernels_per_turn=kernels_per_turn,
-                centroid=(cx, cy))
+                e2e_s=e2e_s, h2d=h2d, d2h=8 * 34,
+                kernels_per_turn=kernels_per_turn, centroid=(cx, cy))
 
 
 def cpu_baseline(w, coords, budget_s=12.0):

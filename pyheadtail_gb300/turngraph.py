@@ -110,3 +110,74 @@ class TurnGraph(object):
         for _ in range(n_graphs):
             self.graph.replay()
         self.beam._engine.touch()
+
+
+class StreamedTurns(object):
+    """A stream of bunches, each copied in from host memory, tracked through
+    its captured turn(s) and read out (its centroid), with the copy of one
+    bunch overlapped with the turns of the previous one.
+
+    ``make(slot)`` builds a (beam, one_turn_map) pair; ``n_slots`` of them
+    (default 2) take the bunches in turn, each with its own captured
+    TurnGraph.  ``push(host_coords)`` queues, on the slot's turn: the
+    host-to-device copy of the six pinned host arrays into the slot's beam
+    on a copy stream (after the slot's previous turn has finished with
+    them), the graph replay on the compute stream (after the copy), a
+    centroid pass (order-1 statistics of x and y) and the device-to-host
+    copy of its record; it returns the centroid (x, y) of the bunch pushed
+    ``n_slots`` calls earlier, or None.  ``drain()`` returns the rest.
+    A beam state carries over in its slot (wake history, pending kick), as
+    in an eager loop that reloads its coordinates."""
+
+    def __init__(self, make, n_slots=2, warmup_turns=3):
+        from .particles import statistics as S
+        self._S = S
+        self.slots = []
+        for k in range(n_slots):
+            beam, otm = make(k)
+            tg = TurnGraph(otm, beam, warmup_turns=warmup_turns).capture()
+            dev = beam._device
+            self.slots.append(dict(
+                beam=beam, tg=tg,
+                rec=torch.zeros(S.RECORD_LEN, dtype=torch.float64, device=dev),
+                host_rec=torch.zeros(S.RECORD_LEN,
+                                     dtype=torch.float64).pin_memory(),
+                copied=torch.cuda.Event(), done=torch.cuda.Event(),
+                busy=False))
+        self.copy_stream = torch.cuda.Stream()
+        self.i = 0
+
+    def _result(self, slot):
+        slot['done'].synchronize()
+        r = self._S.StatsRecord(slot['host_rec'].numpy().copy(), mask=0x5,
+                                order=1)
+        slot['busy'] = False
+        return r.mean('x'), r.mean('y')
+
+    def push(self, host_coords):
+        slot = self.slots[self.i % len(self.slots)]
+        self.i += 1
+        out = self._result(slot) if slot['busy'] else None
+        beam = slot['beam']
+        cs = torch.cuda.current_stream()
+        with torch.cuda.stream(self.copy_stream):
+            self.copy_stream.wait_event(slot['done'])
+            for k, t in host_coords.items():
+                beam._c[k].copy_(t, non_blocking=True)
+            slot['copied'].record(self.copy_stream)
+        beam._engine.touch()
+        cs.wait_event(slot['copied'])
+        slot['tg'].replay(1)
+        beam.launch_stats(slot['rec'], order=1, mask=0x5)
+        slot['host_rec'].copy_(slot['rec'], non_blocking=True)
+        slot['done'].record(cs)
+        slot['busy'] = True
+        return out
+
+    def drain(self):
+        out = []
+        for k in range(len(self.slots)):
+            slot = self.slots[(self.i + k) % len(self.slots)]
+            if slot['busy']:
+                out.append(self._result(slot))
+        return out

@@ -84,3 +84,42 @@ def test_damper_turn_graph_replay(lib):
     torch.cuda.synchronize()
     for k in COORDS:
         assert torch.equal(getattr(eager, k), getattr(graphed, k)), k
+
+
+def test_streamed_turns_match_eager(lib):
+    """turngraph.StreamedTurns (copy of one bunch overlapped with the turn
+    of the previous one, two beams in turn) gives, for every pushed bunch,
+    the centroid an eager loop gives after loading the same coordinates and
+    tracking one turn (zero intensity: no wake kick carries over)."""
+    import cases as C
+    import gpu_cases as G
+    from oracle import cases as OC
+    from pyheadtail_gb300.turngraph import StreamedTurns
+    spec = dict(C.CASES['c1_full'])
+    spec['beam'] = C.beam_params(20000, 0, intensity=0.)
+    bunches = []
+    for seed in range(5):
+        c = OC.make_beam(C.beam_params(20000, 100 + seed)).coords()
+        bunches.append({k: torch.from_numpy(v).pin_memory()
+                        for k, v in c.items()})
+
+    def make(k):
+        b = G.make_beam(spec['beam'], OC.make_beam(spec['beam']).coords())
+        return b, [el for _, el in G.make_elements(spec, b)]
+    st = StreamedTurns(make, n_slots=2)
+    got = []
+    for h in bunches:
+        r = st.push(h)
+        if r is not None:
+            got.append(r)
+    got += st.drain()
+    want = []
+    for h in bunches:
+        b = G.make_beam(spec['beam'], {k: v.numpy() for k, v in h.items()})
+        for _, el in G.make_elements(spec, b):
+            el.track(b)
+        want.append((b.mean_x(), b.mean_y()))
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert abs(g[0] - w[0]) <= 1e-12 * 1e-3 and \
+            abs(g[1] - w[1]) <= 1e-12 * 1e-3, (g, w)
