@@ -181,6 +181,7 @@ class BunchBatch(object):
                 o, n = int(self.offsets[b]), int(self.counts[b])
                 st[o:o + n].copy_(bunch._c[q])
             self.storage[q] = st
+        self._rebinds_seen = None
         for b, bunch in enumerate(bunches):
             o, n = int(self.offsets[b]), int(self.counts[b])
             for q in COORDS:
@@ -192,7 +193,11 @@ class BunchBatch(object):
 
     def check_views(self):
         """Raise if a bunch's coordinates were rebound away from the batch
-        (e.g. ``bunch.x = new_array``)."""
+        (e.g. ``bunch.x = new_array``).  Only bunches whose arrays were
+        replaced since the last check are looked at."""
+        now = [bunch._rebinds for bunch in self.bunches]
+        if now == self._rebinds_seen:
+            return
         for b, bunch in enumerate(self.bunches):
             o = int(self.offsets[b])
             for q in COORDS:
@@ -200,6 +205,7 @@ class BunchBatch(object):
                 if t.data_ptr() != self.storage[q][o:].data_ptr():
                     raise RuntimeError('bunch %d: coordinate %s no longer '
                                        'lives in the batch' % (b, q))
+        self._rebinds_seen = now
 
     def coords_struct(self, storage=None):
         st = self.storage if storage is None else storage
@@ -361,6 +367,7 @@ class BatchedTurn(object):
         self.ring = torch.zeros(nb, self.R, 3, S, dtype=torch.float64,
                                 device=dev)
         self.kicks = torch.zeros(nb, max(self.nk, 1), S, dtype=dt, device=dev)
+        self._pk_cache = None     # PendingKicks naming rows of self.kicks
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         if self.slicer is not None:
             b0 = bt.bunches[0]
@@ -590,16 +597,23 @@ class BatchedTurn(object):
                 self.kicks[b].zero_()
 
     def _leave_kicks(self):
+        # one PendingKick per bunch, made once: it only names the bunch's
+        # rows of the kick tables, which stay the same arrays
+        if self._pk_cache is None and self.nk:
+            self._pk_cache = [
+                E.PendingKick(self.dslicer, [
+                    kick.pending_entry(self.kicks[b, k])
+                    for k, kick in enumerate(self.wakes[b].wake_kicks)])
+                for b in range(len(self.batch.bunches))]
         self._left = {}
         for b, bunch in enumerate(self.batch.bunches):
-            bunch._engine.z_version += 1
-            bunch._engine.touch()
+            eng = bunch._engine
+            eng.z_version += 1
+            eng.touch()
             if self.nk == 0:
                 continue
-            entries = [kick.pending_entry(self.kicks[b, k])
-                       for k, kick in enumerate(self.wakes[b].wake_kicks)]
-            pk = E.PendingKick(self.dslicer, entries)
-            bunch._engine.kick = pk
+            pk = self._pk_cache[b]
+            eng.kick = pk
             self._left[b] = pk
 
     def track(self, n_turns=1):

@@ -62,6 +62,7 @@ class Particles(Printing):
         self._c = {}
         self._engine = E.Engine(self)
         self._exposed = 0          # bumped when a coordinate is handed out
+        self._rebinds = 0          # bumped when a coordinate array is replaced
         self._stats_ws = None
         self._stats_cache = None
         self._stats_mask = 0
@@ -144,6 +145,7 @@ class Particles(Printing):
         self._engine.flush()
         self._engine.z_version += 1
         self._exposed += 1
+        self._rebinds += 1
         t = _as_tensor(value, self._dtype, self._device)
         if t.shape != (self.macroparticlenumber,):
             raise ValueError('lengths of given phase space coordinate arrays '
@@ -199,6 +201,7 @@ class Particles(Printing):
     def reorder(self, permutation, except_for_attrs=[]):
         self._engine.flush()
         self._exposed += 1
+        self._rebinds += 1
         for attr in ['id'] + list(self.coords_n_momenta):
             if attr in except_for_attrs:
                 continue
