@@ -738,36 +738,55 @@ template <>
 struct Bins<float> {
     const float* e;
     int S, neg;
-    float tail, iw, e0, eS;
+    float tail, iw, e0, eS, mg;
+    // mg bounds |u - u_ref|, u = (zz - e0) * iw the FP32 position in slice
+    // units and u_ref the reference's (z - tail) / width of the same z.
+    // The table's end edges lie within one FP32 ulp of the real cuts, so
+    // with A = |e0| + |eS|: |u - u_ref| <= 2^-23 A iw (the cuts) +
+    // 4 * 2^-24 (S + 1) (the four roundings of D = eS - e0, S / D,
+    // zz - e0 and the product), plus FP64 roundings of order 2^-52 S.
+    // mg takes twice that; a margin of 1/4 slice or more switches the fast
+    // path off.
     __device__ __forceinline__ void init(const float* edges, int n, int negate) {
         e = edges; S = n; neg = negate;
         e0 = e[0]; eS = e[S];
         tail = e0;
         const float span = eS - e0;
         iw = span > 0.f ? (float)S / span : 0.f;
+        const float m = 4.76837158203125e-7f *      // 2^-21
+                        ((fabsf(e0) + fabsf(eS)) * iw + (float)S + 2.f);
+        mg = m < 0.25f ? m : 2.f;
     }
-    // Exact slice of VEC particles: every estimate and both bracketing
-    // edges are issued before any correction, so the shared-memory loads of
-    // the VEC lookups overlap.  The corrections walk at most to the table
-    // ends (e0 <= zz < eS holds inside), so no access leaves e[0..S].
+    // Exact slice of VEC particles.  Fast path: when u lies at least mg
+    // inside a slice of [0, S), floor(u) is the reference's index.  Only
+    // particles within mg of a slice edge (or outside the cuts, or NaN)
+    // read the edge table: the estimate and both bracketing edges, then
+    // corrections that walk at most to the table ends (e0 <= zz < eS holds
+    // inside), so no access leaves e[0..S].
     template <int VEC>
     __device__ __forceinline__ void index_vec(const float (&z)[VEC],
                                               int (&out)[VEC]) const {
-        float zz[VEC], lo[VEC], hi[VEC];
-        int k[VEC];
+        float zz[VEC];
+        bool slow = false;
 #pragma unroll
         for (int j = 0; j < VEC; ++j) {
             zz[j] = neg ? -z[j] : z[j];
-            int kk = (int)((zz[j] - tail) * iw);
-            k[j] = kk < 0 ? 0 : (kk > S - 1 ? S - 1 : kk);
+            const float u = (zz[j] - tail) * iw;
+            const float fl = floorf(u);
+            const float fr = u - fl;             // exact
+            const bool ok = fr >= mg && fr <= 1.f - mg && fl >= 0.f &&
+                            fl < (float)S;
+            out[j] = ok ? (int)fl : -2;
+            slow |= !ok;
         }
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) { lo[j] = e[k[j]]; hi[j] = e[k[j] + 1]; }
+        if (!slow) return;
 #pragma unroll
         for (int j = 0; j < VEC; ++j) {
+            if (out[j] != -2) continue;
             if (!(zz[j] >= e0) || !(zz[j] < eS)) { out[j] = -1; continue; }
-            int kk = k[j];
-            float l = lo[j], h = hi[j];
+            int kk = (int)((zz[j] - tail) * iw);
+            kk = kk < 0 ? 0 : (kk > S - 1 ? S - 1 : kk);
+            float l = e[kk], h = e[kk + 1];
             while (zz[j] < l) { --kk; h = l; l = e[kk]; }
             while (zz[j] >= h) { ++kk; h = e[kk + 1]; }
             out[j] = kk;

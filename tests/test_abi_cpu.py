@@ -163,3 +163,60 @@ def test_exact_edges_reproduce_reference_index(code, cuts, S):
     got = np.searchsorted(e, u, side='right') - 1
     assert np.array_equal(inside, (want >= 0) & (want < S))
     assert np.array_equal(got[inside], want[inside].astype(np.int64))
+
+
+def _fast_bin_f32(u, e):
+    """The FP32 lookup's table-free path (Bins<float>::index_vec in
+    csrc/phk_track.cuh), evaluated with the same float32 roundings:
+    returns the index floor(u) and whether the path is taken."""
+    f = np.float32
+    S = len(e) - 1
+    e0, eS = e[0], e[S]
+    span = f(eS - e0)
+    iw = f(f(S) / span) if span > 0 else f(0)
+    m = f(f(2.0 ** -21) * f(f(f(abs(e0)) + f(abs(eS))) * iw + f(S) + f(2)))
+    mg = m if m < f(0.25) else f(2)
+    uu = (u.astype(np.float32) - e0).astype(np.float32) * iw
+    fl = np.floor(uu)
+    fr = uu - fl
+    ok = (fr >= mg) & (fr <= f(1) - mg) & (fl >= 0) & (fl < S)
+    return fl.astype(np.int64), ok, mg
+
+
+@pytest.mark.parametrize('cuts,S', [((-0.69, 0.69), 500), ((-0.69, 0.69), 1000),
+                                    ((-0.69, 0.69), 100), ((-0.31, 0.05), 7),
+                                    ((0.2, -0.2), 13), ((-3e-3, 1e-2), 500),
+                                    ((-1.1, 1.3), 1000), ((99.5, 100.5), 64),
+                                    ((-1e-6, 1e-6), 1000), ((0.0, 2.0), 4096)])
+def test_fp32_fast_bin_path_is_exact(cuts, S):
+    """Wherever the table-free path is taken, floor(u) equals the
+    reference's int(floor((z - tail) / width)) -- checked on random z, on
+    every edge and its float neighbours, and on points a few ulps around
+    every interior boundary, where the margin is what keeps it exact."""
+    from pyheadtail_gb300 import _engine as E
+    tail, head = cuts
+    width = (head - tail) / float(S)
+    e, neg = E.exact_edges(tail, width, S, 1)
+    rng = np.random.RandomState(S + 7)
+    span = abs(head - tail)
+    z = rng.uniform(min(tail, head) - 0.1 * span, max(tail, head) + 0.1 * span,
+                    400000).astype(np.float32)
+    z = np.concatenate([z, rng.normal(0.5 * (tail + head), 0.2 * span,
+                                      400000).astype(np.float32)])
+    ez = (-e if neg else e).astype(np.float32)
+    near = [ez]
+    lo, hi = ez.copy(), ez.copy()
+    for _ in range(8):
+        lo = np.nextafter(lo, np.float32(-np.inf))
+        hi = np.nextafter(hi, np.float32(np.inf))
+        near += [lo, hi]
+    z = np.concatenate([z] + near)
+    want = np.floor((z.astype(np.float64) - tail) / width)
+    u = -z if neg else z
+    k, ok, mg = _fast_bin_f32(u, e)
+    inside = (want >= 0) & (want < S)
+    assert np.all(inside[ok])
+    assert np.array_equal(k[ok], want[ok].astype(np.int64))
+    if mg < 0.25 and span / S > 1e-5:
+        # the fast path serves all but particles within mg of an edge
+        assert ok[:800000].mean() > 1 - 4 * float(mg) - 0.25, ok.mean()

@@ -236,36 +236,56 @@ def test_all_outside_and_empty_slices(lib):
     assert int((ss.slice_index_of_particle >= 0).sum()) == n   # 5 * 20 / 1.38
 
 
+@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
 @pytest.mark.parametrize('n,S', [(10**7, 500), (5 * 10**7, 1000)])
-def test_full_size_binning_bit_exact(lib, n, S):
+def test_full_size_binning_bit_exact(lib, n, S, precision):
     """C3 / C5 sizes: every particle's slice index equals the reference
-    formula int32(floor((z - tail)/width)) evaluated by torch in FP64."""
+    formula int32(floor((z - tail)/width)) evaluated by torch in FP64 on
+    the form's own z.  The first particles sit on every slice edge and on
+    the 8 representable values either side of it, where the FP32 lookup's
+    table-free path must hand over to the edge table."""
     import gpu_cases as G
     import cases as C
-    from pyheadtail_gb300.particles.generators import \
-        gaussian_bunch_coordinates
+    from pyheadtail_gb300 import _engine as E
     torch.manual_seed(0)
+    tail, head = C.Z_CUTS
+    width = (head - tail) / float(S)
     z = torch.randn(n, dtype=torch.float64, device='cuda') * 0.23
+    code = E._F64 if precision == 'fp64' else E._F32
+    edges, _ = E.exact_edges(tail, width, S, code)
+    near = [edges]
+    lo, hi = edges.copy(), edges.copy()
+    for _ in range(8):
+        lo = np.nextafter(lo, lo.dtype.type(-np.inf))
+        hi = np.nextafter(hi, hi.dtype.type(np.inf))
+        near += [lo, hi]
+    near = np.concatenate(near).astype(np.float64)
+    z[:len(near)] = torch.from_numpy(near).cuda()
     coords = {k: torch.zeros(n, dtype=torch.float64, device='cuda')
               for k in COORDS}
     coords['z'] = z
     coords['x'] = torch.randn(n, dtype=torch.float64, device='cuda') * 1e-3
-    beam = G.make_beam(C.beam_params(n, 2), coords)
+    beam = G.make_beam(C.beam_params(n, 2), coords, precision=precision)
+    assert beam.z.dtype == (torch.float64 if code == E._F64 else torch.float32)
     sl = G.make_slicer(C.slicer(S))
     ss = sl.slice(beam, statistics=['mean_x', 'mean_y'])
     idx = ss.slice_index_of_particle
-    tail, head = C.Z_CUTS
-    width = (head - tail) / float(S)
-    want = torch.floor((beam.z - tail) / width).to(torch.int32)
+    # NumPy's IEEE division on the host: torch on the GPU divides by a
+    # Python scalar as a multiplication by its reciprocal, which differs
+    # from the reference formula by one ulp exactly at slice edges
+    zh = beam.z.double().cpu().numpy()
+    want = torch.from_numpy(
+        np.floor((zh - tail) / width).astype(np.int32)).cuda()
     assert torch.equal(idx, want)
     inside = (want >= 0) & (want < S)
     counts = torch.bincount(want[inside].long(), minlength=S).to(torch.int32)
     assert torch.equal(ss.n_macroparticles_per_slice, counts)
     sums = torch.zeros(S, dtype=torch.float64, device='cuda')
-    sums.index_add_(0, want[inside].long(), beam.x[inside])
+    sums.index_add_(0, want[inside].long(), beam.x[inside].double())
     mean = torch.where(counts > 0, sums / counts.clamp(min=1).double(),
                        torch.zeros_like(sums))
-    assert float((mean - ss.mean_x).abs().max()) <= 1e-12 * float(
+    tol = 1e-12 if precision == 'fp64' else 1e-5   # FP32 slice sums
+    assert float((mean - ss.mean_x).abs().max()) <= tol * float(
         mean.abs().max())
 
 
