@@ -19,6 +19,9 @@ int program_shape(const phk_program* prog) {
     int k[4] = {0, 0, 0, 0};
     for (int i = 0; i < n && i < 4; ++i) k[i] = prog->op[i].kind;
     if (n == 0) return SHAPE_NONE;
+    // the shapes read op[0]'s detuners from det[0] on
+    if (k[0] == PHK_OP_TRANSVERSE && prog->op[0].det_begin != 0)
+        return SHAPE_GENERIC;
     if (n == 1 && k[0] == PHK_OP_TRANSVERSE) return SHAPE_T;
     if (n == 2 && k[0] == PHK_OP_TRANSVERSE && k[1] == PHK_OP_LINEAR_LONG)
         return SHAPE_T_LIN;

@@ -61,7 +61,8 @@ __device__ __forceinline__ double ij_term(double I, double J, bool hi,
     return 0.0;
 }
 
-template <int VEC>
+// OP0 (unused here): see the FP32 form
+template <int VEC, bool OP0 = false>
 __device__ __forceinline__ void op_transverse(const phk_op& op,
                                               const phk_program& prog,
                                               Tile<double, VEC>& t) {
@@ -278,7 +279,67 @@ __device__ __forceinline__ float chroma_poly_f32(const float* c, int n, int z,
     return r;
 }
 
+// dq += the chromatic detuning of VEC particles (ChromaticitySegment.detune,
+// trackers/detuners.py:64-98): Horner orders 1-3 inline, anything else
+// through the general loop.  The branches are uniform.
 template <int VEC>
+__device__ __forceinline__ void chroma_add_f32(const float* c, int n, int z,
+                                               const float (&dp)[VEC],
+                                               float (&dq)[VEC]) {
+    if (z == 0 && n == 1) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dq[j] = fmaf(c[0], dp[j], dq[j]);
+    } else if (z == 0 && n == 2) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+            dq[j] = fmaf(fmaf(c[1], dp[j], c[0]), dp[j], dq[j]);
+    } else if (z == 0 && n == 3) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+            dq[j] = fmaf(fmaf(fmaf(c[2], dp[j], c[1]), dp[j], c[0]), dp[j],
+                         dq[j]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dq[j] += chroma_poly_f32(c, n, z, dp[j]);
+    }
+}
+
+// dqx, dqy += the detuning of VEC particles by one detuner
+template <int VEC>
+__device__ __forceinline__ void detune_f32(const phk_detuner& dt,
+                                           const Tile<float, VEC>& t,
+                                           float (&dqx)[VEC],
+                                           float (&dqy)[VEC]) {
+    const float* c = reinterpret_cast<const float*>(dt.c);
+    if (dt.kind == PHK_DET_CHROMA) {
+        chroma_add_f32<VEC>(c, dt.nx, dt.zx, t.c[PHK_DP], dqx);
+        chroma_add_f32<VEC>(c + 8, dt.ny, dt.zy, t.c[PHK_DP], dqy);
+    } else {
+        // c = dapp_x/p0, dapp_y/p0, dapp_xy/p0, dapp_yx/p0,
+        //     (1+ax^2)/bx, 2ax, bx, (1+ay^2)/by, 2ay, by
+        const float ax = c[0], ay = c[1], axy = c[2], ayx = c[3];
+        const float c1x = c[4], tax = c[5], bx = c[6];
+        const float c1y = c[7], tay = c[8], by = c[9];
+        const float (&x)[VEC] = t.c[PHK_X];
+        const float (&xp)[VEC] = t.c[PHK_XP];
+        const float (&y)[VEC] = t.c[PHK_Y];
+        const float (&yp)[VEC] = t.c[PHK_YP];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const float Jx = 0.5f * fmaf(bx * xp[j], xp[j],
+                                         fmaf(tax * x[j], xp[j], c1x * x[j] * x[j]));
+            const float Jy = 0.5f * fmaf(by * yp[j], yp[j],
+                                         fmaf(tay * y[j], yp[j], c1y * y[j] * y[j]));
+            dqx[j] += fmaf(ax, Jx, axy * Jy);
+            dqy[j] += fmaf(ay, Jy, ayx * Jx);
+        }
+    }
+}
+
+// OP0: the op is prog.op[0] of a specialised shape, whose detuners start at
+// det[0] (program_shape checks it), so the first two are read at
+// compile-time offsets of the parameter block.
+template <int VEC, bool OP0 = false>
 __device__ __forceinline__ void op_transverse(const phk_op& op,
                                               const phk_program& prog,
                                               Tile<float, VEC>& t) {
@@ -295,32 +356,14 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
         float dqx[VEC], dqy[VEC];
 #pragma unroll
         for (int j = 0; j < VEC; ++j) { dqx[j] = 0.f; dqy[j] = 0.f; }
-        for (int d = 0; d < op.det_count; ++d) {
-            const phk_detuner& dt = prog.det[op.det_begin + d];
-            const float* c = reinterpret_cast<const float*>(dt.c);
-            if (dt.kind == PHK_DET_CHROMA) {
-                const int nx = dt.nx, ny = dt.ny, zx = dt.zx, zy = dt.zy;
-#pragma unroll
-                for (int j = 0; j < VEC; ++j) {
-                    dqx[j] += chroma_poly_f32(c, nx, zx, dp[j]);
-                    dqy[j] += chroma_poly_f32(c + 8, ny, zy, dp[j]);
-                }
-            } else {
-                // c = dapp_x/p0, dapp_y/p0, dapp_xy/p0, dapp_yx/p0,
-                //     (1+ax^2)/bx, 2ax, bx, (1+ay^2)/by, 2ay, by
-                const float ax = c[0], ay = c[1], axy = c[2], ayx = c[3];
-                const float c1x = c[4], tax = c[5], bx = c[6];
-                const float c1y = c[7], tay = c[8], by = c[9];
-#pragma unroll
-                for (int j = 0; j < VEC; ++j) {
-                    const float Jx = 0.5f * fmaf(bx * xp[j], xp[j],
-                                                 fmaf(tax * x[j], xp[j], c1x * x[j] * x[j]));
-                    const float Jy = 0.5f * fmaf(by * yp[j], yp[j],
-                                                 fmaf(tay * y[j], yp[j], c1y * y[j] * y[j]));
-                    dqx[j] += fmaf(ax, Jx, axy * Jy);
-                    dqy[j] += fmaf(ay, Jy, ayx * Jx);
-                }
-            }
+        const int nd = op.det_count;
+        if (OP0) {
+            if (nd > 0) detune_f32<VEC>(prog.det[0], t, dqx, dqy);
+            if (nd > 1) detune_f32<VEC>(prog.det[1], t, dqx, dqy);
+            for (int d = 2; d < nd; ++d) detune_f32<VEC>(prog.det[d], t, dqx, dqy);
+        } else {
+            for (int d = 0; d < nd; ++d)
+                detune_f32<VEC>(prog.det[op.det_begin + d], t, dqx, dqy);
         }
         const float qxh = p[16], qxl = p[17], qyh = p[18], qyl = p[19];
 #pragma unroll
@@ -508,14 +551,14 @@ __device__ __forceinline__ void run_program_shape(const phk_program& prog,
     if constexpr (SHAPE == SHAPE_NONE) {
         return;
     } else if constexpr (SHAPE == SHAPE_T) {
-        op_transverse<VEC>(prog.op[0], prog, t);
+        op_transverse<VEC, true>(prog.op[0], prog, t);
     } else if constexpr (SHAPE == SHAPE_T_RF) {
-        op_transverse<VEC>(prog.op[0], prog, t);
+        op_transverse<VEC, true>(prog.op[0], prog, t);
         op_drift<VEC>(prog.op[1], t);
         op_rfkick<VEC>(prog.op[2], t);
         op_drift<VEC>(prog.op[3], t);
     } else if constexpr (SHAPE == SHAPE_T_LIN) {
-        op_transverse<VEC>(prog.op[0], prog, t);
+        op_transverse<VEC, true>(prog.op[0], prog, t);
         op_linear_long<VEC>(prog.op[1], t);
     } else {
         run_program<T, VEC>(prog, t);
@@ -774,9 +817,10 @@ struct Bins<float> {
             const float u = (zz[j] - tail) * iw;
             const float fl = floorf(u);
             const float fr = u - fl;             // exact
-            const bool ok = fr >= mg && fr <= 1.f - mg && fl >= 0.f &&
-                            fl < (float)S;
-            out[j] = ok ? (int)fl : -2;
+            const int ki = (int)fl;              // saturating, NaN -> 0
+            const bool ok = fr >= mg && fr <= 1.f - mg &&
+                            (unsigned)ki < (unsigned)S;
+            out[j] = ok ? ki : -2;
             slow |= !ok;
         }
         if (!slow) return;
