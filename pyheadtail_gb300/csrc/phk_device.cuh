@@ -266,4 +266,81 @@ __device__ __forceinline__ float sin_turns_of_product(float z, float mh,
     return s;
 }
 
+// ------------------------------------------- packed FP32 pairs (f32x2)
+// Two particles per instruction on the sm_100 family's paired FP32 pipes
+// (FFMA2 / FADD2 / FMUL2).  Each lane is rounded exactly as the scalar
+// fmaf / + / * it stands for, so the packed forms below return, lane for
+// lane, the bits of their scalar counterparts above.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    return __ffma2_rn(a, b, c);
+}
+// a - b, one rounding (b * -1 is exact)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+}
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// quadrant rotation of sincos_2pi for one lane
+__device__ __forceinline__ void quadrant_2pi(float q, float sn, float cs,
+                                             float* s, float* c) {
+    const int k = (int)q & 3;
+    const float a = (k & 1) ? cs : sn;
+    const float b = (k & 1) ? sn : cs;
+    *s = (k & 2) ? -a : a;
+    *c = ((k + 1) & 2) ? -b : b;
+}
+
+// sincos_2pi of two lanes
+__device__ __forceinline__ void sincos_2pi_x2(float2 f, float2* s, float2* c) {
+    const float2 q = make_float2(rintf(4.0f * f.x), rintf(4.0f * f.y));
+    const float2 r = fma2(f2(-0.25f), q, f);
+    const float2 th = fma2(r, f2(6.28318548202514648438f),
+                           mul2(r, f2(-1.7484556e-7f)));
+    const float2 t2 = mul2(th, th);
+    float2 ps = fma2(t2, f2(-2.5052108385e-8f), f2(2.7557319224e-6f));
+    ps = fma2(t2, ps, f2(-1.9841269841e-4f));
+    ps = fma2(t2, ps, f2(8.3333333333e-3f));
+    ps = fma2(t2, ps, f2(-1.6666666667e-1f));
+    const float2 sn = fma2(mul2(th, t2), ps, th);
+    float2 pc = fma2(t2, f2(-2.7557319224e-7f), f2(2.4801587302e-5f));
+    pc = fma2(t2, pc, f2(-1.3888888889e-3f));
+    pc = fma2(t2, pc, f2(4.1666666667e-2f));
+    pc = fma2(t2, pc, f2(-0.5f));
+    const float2 cs = fma2(t2, pc, f2(1.0f));
+    quadrant_2pi(q.x, sn.x, cs.x, &s->x, &c->x);
+    quadrant_2pi(q.y, sn.y, cs.y, &s->y, &c->y);
+}
+
+// sincos_turns of two lanes, the float-float base given per lane
+__device__ __forceinline__ void sincos_turns_x2(float2 hi, float2 lo, float2 d,
+                                                float2* s, float2* c) {
+    const float2 t = add2(hi, d);
+    const float2 bp = sub2(t, hi);
+    float2 err = add2(sub2(hi, sub2(t, bp)), sub2(d, bp));
+    err = add2(err, lo);
+    const float2 r = sub2(t, make_float2(rintf(t.x), rintf(t.y)));
+    const float2 f = add2(r, err);
+    const float2 g = add2(sub2(r, f), err);
+    float2 sp, cp;
+    sincos_2pi_x2(f, &sp, &cp);
+    const float2 dl = mul2(f2(6.28318530717958647692f), g);
+    *s = fma2(dl, cp, sp);
+    *c = fma2(neg2(dl), sp, cp);
+}
+
+// sin_turns_of_product of two lanes
+__device__ __forceinline__ float2 sin_turns_of_product_x2(float2 z, float mh,
+                                                          float ml, float oh,
+                                                          float ol) {
+    const float2 p = mul2(z, f2(mh));
+    float2 e = fma2(z, f2(mh), neg2(p));
+    e = fma2(z, f2(ml), e);
+    float2 s, c;
+    sincos_turns_x2(p, add2(e, f2(ol)), f2(oh), &s, &c);
+    return s;
+}
+
 }  // namespace phk

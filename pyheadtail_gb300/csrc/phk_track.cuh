@@ -339,10 +339,84 @@ __device__ __forceinline__ void detune_f32(const phk_detuner& dt,
 // OP0: the op is prog.op[0] of a specialised shape, whose detuners start at
 // det[0] (program_shape checks it), so the first two are read at
 // compile-time offsets of the parameter block.
+// op_transverse for two particles per thread on the paired FP32 pipes:
+// the same operations as the scalar form below, lane for lane
+template <bool OP0>
+__device__ __forceinline__ void op_transverse_x2(const phk_op& op,
+                                                 const phk_program& prog,
+                                                 Tile<float, 2>& t) {
+    const float* p = reinterpret_cast<const float*>(op.p);
+    const bool disp = op.flags & PHK_FLAG_DISPERSION;
+    float2 X = make_float2(t.c[PHK_X][0], t.c[PHK_X][1]);
+    float2 XP = make_float2(t.c[PHK_XP][0], t.c[PHK_XP][1]);
+    float2 Y = make_float2(t.c[PHK_Y][0], t.c[PHK_Y][1]);
+    float2 YP = make_float2(t.c[PHK_YP][0], t.c[PHK_YP][1]);
+    const float2 DP = make_float2(t.c[PHK_DP][0], t.c[PHK_DP][1]);
+    float2 M[8];
+    const bool detuned = op.flags & PHK_FLAG_DETUNED;
+    if (detuned) {
+        float dqx[2] = {0.f, 0.f}, dqy[2] = {0.f, 0.f};
+        const int nd = op.det_count;
+        if (OP0) {
+            if (nd > 0) detune_f32<2>(prog.det[0], t, dqx, dqy);
+            if (nd > 1) detune_f32<2>(prog.det[1], t, dqx, dqy);
+            for (int d = 2; d < nd; ++d) detune_f32<2>(prog.det[d], t, dqx, dqy);
+        } else {
+            for (int d = 0; d < nd; ++d)
+                detune_f32<2>(prog.det[op.det_begin + d], t, dqx, dqy);
+        }
+        float2 sx, cx, sy, cy;
+        sincos_turns_x2(f2(p[16]), f2(p[17]), make_float2(dqx[0], dqx[1]), &sx, &cx);
+        sincos_turns_x2(f2(p[18]), f2(p[19]), make_float2(dqy[0], dqy[1]), &sy, &cy);
+        // I and J are float-float (p[40..55] their low parts)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            M[e] = fma2(f2(p[e]), cx,
+                        fma2(f2(p[8 + e]), sx,
+                             fma2(f2(p[40 + e]), cx, mul2(f2(p[48 + e]), sx))));
+            M[4 + e] = fma2(f2(p[4 + e]), cy,
+                            fma2(f2(p[12 + e]), sy,
+                                 fma2(f2(p[44 + e]), cy, mul2(f2(p[52 + e]), sy))));
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) M[e] = f2(p[e]);
+    }
+    if (disp) {
+        X = fma2(f2(-p[32]), DP, X);
+        Y = fma2(f2(-p[34]), DP, Y);
+    }
+    float2 cxr = f2(0.f), cxp = f2(0.f), cyr = f2(0.f), cyp = f2(0.f);
+    if (!detuned) {
+        // low parts of the constant matrix
+        cxr = fma2(f2(p[40]), X, mul2(f2(p[41]), XP));
+        cxp = fma2(f2(p[42]), X, mul2(f2(p[43]), XP));
+        cyr = fma2(f2(p[44]), Y, mul2(f2(p[45]), YP));
+        cyp = fma2(f2(p[46]), Y, mul2(f2(p[47]), YP));
+    }
+    const float2 nx = fma2(M[0], X, fma2(M[1], XP, cxr));
+    const float2 nxp = fma2(M[2], X, fma2(M[3], XP, cxp));
+    const float2 ny = fma2(M[4], Y, fma2(M[5], YP, cyr));
+    const float2 nyp = fma2(M[6], Y, fma2(M[7], YP, cyp));
+    X = nx; XP = nxp; Y = ny; YP = nyp;
+    if (disp) {
+        X = fma2(f2(p[33]), DP, X);
+        Y = fma2(f2(p[35]), DP, Y);
+    }
+    t.c[PHK_X][0] = X.x; t.c[PHK_X][1] = X.y;
+    t.c[PHK_XP][0] = XP.x; t.c[PHK_XP][1] = XP.y;
+    t.c[PHK_Y][0] = Y.x; t.c[PHK_Y][1] = Y.y;
+    t.c[PHK_YP][0] = YP.x; t.c[PHK_YP][1] = YP.y;
+}
+
 template <int VEC, bool OP0 = false>
 __device__ __forceinline__ void op_transverse(const phk_op& op,
                                               const phk_program& prog,
                                               Tile<float, VEC>& t) {
+    if constexpr (VEC == 2) {
+        op_transverse_x2<OP0>(op, prog, t);
+        return;
+    }
     const float* p = reinterpret_cast<const float*>(op.p);
     const bool disp = op.flags & PHK_FLAG_DISPERSION;
     const float Dx0 = p[32], Dx1 = p[33], Dy0 = p[34], Dy1 = p[35];
@@ -421,6 +495,14 @@ __device__ __forceinline__ void op_drift(const phk_op& op,
     const float* p = reinterpret_cast<const float*>(op.p);
     const float br = p[0], etaL = p[1], etaLl = p[2], brl = p[3];
     const bool shrink = op.flags & PHK_FLAG_SHRINK;
+    if constexpr (VEC == 2) {
+        const float2 Z = make_float2(t.c[PHK_Z][0], t.c[PHK_Z][1]);
+        const float2 DP = make_float2(t.c[PHK_DP][0], t.c[PHK_DP][1]);
+        const float2 zs = shrink ? fma2(f2(br), Z, mul2(f2(brl), Z)) : Z;
+        const float2 zn = fma2(f2(-etaL), DP, fma2(f2(-etaLl), DP, zs));
+        t.c[PHK_Z][0] = zn.x; t.c[PHK_Z][1] = zn.y;
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
         // z = beta_ratio * z - (eta0 * L) * dp, constants float-float
@@ -442,6 +524,27 @@ __device__ __forceinline__ void op_rfkick(const phk_op& op,
     const float A = p[4], ratio = p[5], pinc = p[6], Dx = p[8], Dy = p[9];
     const float Al = p[10], ratiol = p[11];
     const bool disp = op.flags & PHK_FLAG_DISPERSION;
+    if constexpr (VEC == 2) {
+        float2 DP = make_float2(t.c[PHK_DP][0], t.c[PHK_DP][1]);
+        float2 X = make_float2(t.c[PHK_X][0], t.c[PHK_X][1]);
+        float2 Y = make_float2(t.c[PHK_Y][0], t.c[PHK_Y][1]);
+        if (disp) {
+            X = fma2(f2(-Dx), DP, X);
+            Y = fma2(f2(-Dy), DP, Y);
+        }
+        const float2 s = sin_turns_of_product_x2(
+            make_float2(t.c[PHK_Z][0], t.c[PHK_Z][1]), mh, ml, oh, ol);
+        DP = fma2(f2(A), s, fma2(f2(Al), s,
+                                 fma2(DP, f2(ratio), fma2(DP, f2(ratiol), f2(-pinc)))));
+        if (disp) {
+            X = fma2(f2(Dx), DP, X);
+            Y = fma2(f2(Dy), DP, Y);
+        }
+        t.c[PHK_DP][0] = DP.x; t.c[PHK_DP][1] = DP.y;
+        t.c[PHK_X][0] = X.x; t.c[PHK_X][1] = X.y;
+        t.c[PHK_Y][0] = Y.x; t.c[PHK_Y][1] = Y.y;
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < VEC; ++j) {
         float& dp = t.c[PHK_DP][j];
