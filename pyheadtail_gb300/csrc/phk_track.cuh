@@ -339,6 +339,48 @@ __device__ __forceinline__ void detune_f32(const phk_detuner& dt,
 // OP0: the op is prog.op[0] of a specialised shape, whose detuners start at
 // det[0] (program_shape checks it), so the first two are read at
 // compile-time offsets of the parameter block.
+// detune_f32 of two particles on the paired FP32 pipes
+__device__ __forceinline__ void detune_f32_x2(const phk_detuner& dt,
+                                              const Tile<float, 2>& t,
+                                              float2& dqx, float2& dqy) {
+    const float* c = reinterpret_cast<const float*>(dt.c);
+    const float2 DP = make_float2(t.c[PHK_DP][0], t.c[PHK_DP][1]);
+    if (dt.kind == PHK_DET_CHROMA) {
+        const int n[2] = {dt.nx, dt.ny}, z[2] = {dt.zx, dt.zy};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const float* cq = c + 8 * q;
+            float2& dq = q ? dqy : dqx;
+            if (z[q] == 0 && n[q] == 1) {
+                dq = fma2(f2(cq[0]), DP, dq);
+            } else if (z[q] == 0 && n[q] == 2) {
+                dq = fma2(fma2(f2(cq[1]), DP, f2(cq[0])), DP, dq);
+            } else if (z[q] == 0 && n[q] == 3) {
+                dq = fma2(fma2(fma2(f2(cq[2]), DP, f2(cq[1])), DP, f2(cq[0])),
+                          DP, dq);
+            } else {
+                dq.x += chroma_poly_f32(cq, n[q], z[q], DP.x);
+                dq.y += chroma_poly_f32(cq, n[q], z[q], DP.y);
+            }
+        }
+    } else {
+        const float2 X = make_float2(t.c[PHK_X][0], t.c[PHK_X][1]);
+        const float2 XP = make_float2(t.c[PHK_XP][0], t.c[PHK_XP][1]);
+        const float2 Y = make_float2(t.c[PHK_Y][0], t.c[PHK_Y][1]);
+        const float2 YP = make_float2(t.c[PHK_YP][0], t.c[PHK_YP][1]);
+        const float2 Jx = mul2(f2(0.5f),
+                               fma2(mul2(f2(c[6]), XP), XP,
+                                    fma2(mul2(f2(c[5]), X), XP,
+                                         mul2(mul2(f2(c[4]), X), X))));
+        const float2 Jy = mul2(f2(0.5f),
+                               fma2(mul2(f2(c[9]), YP), YP,
+                                    fma2(mul2(f2(c[8]), Y), YP,
+                                         mul2(mul2(f2(c[7]), Y), Y))));
+        dqx = add2(dqx, fma2(f2(c[0]), Jx, mul2(f2(c[2]), Jy)));
+        dqy = add2(dqy, fma2(f2(c[1]), Jy, mul2(f2(c[3]), Jx)));
+    }
+}
+
 // op_transverse for two particles per thread on the paired FP32 pipes:
 // the same operations as the scalar form below, lane for lane
 template <bool OP0>
@@ -355,19 +397,19 @@ __device__ __forceinline__ void op_transverse_x2(const phk_op& op,
     float2 M[8];
     const bool detuned = op.flags & PHK_FLAG_DETUNED;
     if (detuned) {
-        float dqx[2] = {0.f, 0.f}, dqy[2] = {0.f, 0.f};
+        float2 dqx = f2(0.f), dqy = f2(0.f);
         const int nd = op.det_count;
         if (OP0) {
-            if (nd > 0) detune_f32<2>(prog.det[0], t, dqx, dqy);
-            if (nd > 1) detune_f32<2>(prog.det[1], t, dqx, dqy);
-            for (int d = 2; d < nd; ++d) detune_f32<2>(prog.det[d], t, dqx, dqy);
+            if (nd > 0) detune_f32_x2(prog.det[0], t, dqx, dqy);
+            if (nd > 1) detune_f32_x2(prog.det[1], t, dqx, dqy);
+            for (int d = 2; d < nd; ++d) detune_f32_x2(prog.det[d], t, dqx, dqy);
         } else {
             for (int d = 0; d < nd; ++d)
-                detune_f32<2>(prog.det[op.det_begin + d], t, dqx, dqy);
+                detune_f32_x2(prog.det[op.det_begin + d], t, dqx, dqy);
         }
         float2 sx, cx, sy, cy;
-        sincos_turns_x2(f2(p[16]), f2(p[17]), make_float2(dqx[0], dqx[1]), &sx, &cx);
-        sincos_turns_x2(f2(p[18]), f2(p[19]), make_float2(dqy[0], dqy[1]), &sy, &cy);
+        sincos_turns_x2(f2(p[16]), f2(p[17]), dqx, &sx, &cx);
+        sincos_turns_x2(f2(p[18]), f2(p[19]), dqy, &sy, &cy);
         // I and J are float-float (p[40..55] their low parts)
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
