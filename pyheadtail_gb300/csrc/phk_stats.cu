@@ -255,6 +255,7 @@ stats_kernel(const __grid_constant__ phk_kick_set pk,
     __syncthreads();
     Bins<T> bpk;
     if (ta.has_pk) bpk.init(epk, Sp, pk.slicer.negate);
+    vote_fast_path<T>(bpk, ta.has_pk, tid, kStatsThreads);
     const T* cp[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) cp[q] = reinterpret_cast<const T*>(ta.c[q]);

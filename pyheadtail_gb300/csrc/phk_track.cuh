@@ -945,6 +945,20 @@ struct Bins<float> {
                         ((fabsf(e0) + fabsf(eS)) * iw + (float)S + 2.f);
         mg = m < 0.25f ? m : 2.f;
     }
+    // The fast path also needs every edge within mg of its uniform
+    // position: u(e_k) within mg of k.  Then for u at least mg inside
+    // slice k (and u monotone in z), e_k <= z < e_{k+1}.  Tables of
+    // uniform-bin slicers pass (the bound above); tables of other slicers
+    // (uniform charge) fail and keep the search.  u - k is exact here
+    // (Sterbenz) whenever it is small.
+    __device__ __forceinline__ bool edges_uniform(int tid, int nthreads) const {
+        if (mg >= 1.f) return true;
+        bool ok = true;
+        for (int i = tid; i <= S; i += nthreads)
+            ok = ok && fabsf((e[i] - tail) * iw - (float)i) < mg;
+        return ok;
+    }
+    __device__ __forceinline__ void disable_fast() { mg = 2.f; }
     // Exact slice of VEC particles.  Fast path: when u lies at least mg
     // inside a slice of [0, S), floor(u) is the reference's index.  Only
     // particles within mg of a slice edge (or outside the cuts, or NaN)
@@ -1034,7 +1048,20 @@ struct Bins<double> {
         index_vec<1>(zv, o);
         return o[0];
     }
+    // no table-free path in the FP64 form
+    __device__ __forceinline__ bool edges_uniform(int, int) const { return true; }
+    __device__ __forceinline__ void disable_fast() {}
 };
+
+// After Bins::init over a staged table: the table-free lookup stays on
+// only if every edge passes edges_uniform (a block-wide vote; every
+// thread of the block calls this, `active` being the same for all).
+template <typename T>
+__device__ __forceinline__ void vote_fast_path(Bins<T>& b, bool active,
+                                               int tid, int nthreads) {
+    const bool ok = !active || b.edges_uniform(tid, nthreads);
+    if (!__syncthreads_and(ok) && active) b.disable_fast();
+}
 
 // Stages the pending kicks' slice edges (as lookup keys) into `epk` and,
 // when a.kicks_smem, their tables into `ktab`: one table per kick, or with
@@ -1262,6 +1289,8 @@ track_kernel(const __grid_constant__ phk_program prog,
     for (int q = 0; q < 6; ++q) cx.cp[q] = reinterpret_cast<T*>(a.c[q]);
     if (a.has_pk) cx.bpk.init(epk, Sp, pk.slicer.negate);
     if (a.has_acc) cx.bac.init(eacc, Sa, acc.slicer.negate);
+    vote_fast_path<T>(cx.bpk, a.has_pk, tid, blockDim.x);
+    vote_fast_path<T>(cx.bac, a.has_acc, tid, blockDim.x);
     cx.ktab = ktab;
     const int h = (a.n_hist > 1) ? (tid >> 5) % a.n_hist : 0;
     cx.hx = hsx + h * Sa;
@@ -1702,6 +1731,8 @@ batch_track_kernel(const __grid_constant__ phk_kick_set pk,
     __syncthreads();
     if (a.has_pk) cx.bpk.init(epk, Sp, pk.slicer.negate);
     if (a.has_acc) cx.bac.init(eacc, Sa, acc.slicer.negate);
+    vote_fast_path<T>(cx.bpk, a.has_pk, tid, blockDim.x);
+    vote_fast_path<T>(cx.bac, a.has_acc, tid, blockDim.x);
 
     int u0 = b.cta_first[blockIdx.x], u1 = b.cta_first[blockIdx.x + 1];
     if (u0 < 0 || u1 > b.n_units || u0 > u1) {

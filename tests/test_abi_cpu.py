@@ -220,3 +220,34 @@ def test_fp32_fast_bin_path_is_exact(cuts, S):
     if mg < 0.25 and span / S > 1e-5:
         # the fast path serves all but particles within mg of an edge
         assert ok[:800000].mean() > 1 - 4 * float(mg) - 0.25, ok.mean()
+
+
+def _edges_uniform_f32(e, mg):
+    """Bins<float>::edges_uniform: every edge within mg of its uniform
+    position, in the device's float32 roundings."""
+    f = np.float32
+    S = len(e) - 1
+    span = f(e[S] - e[0])
+    iw = f(f(S) / span) if span > 0 else f(0)
+    u = (e.astype(np.float32) - e[0]).astype(np.float32) * iw
+    return bool(np.all(np.abs(u - np.arange(S + 1, dtype=np.float32)) < mg))
+
+
+@pytest.mark.parametrize('cuts,S', [((-0.69, 0.69), 500), ((-0.69, 0.69), 1000),
+                                    ((-0.31, 0.05), 7), ((0.2, -0.2), 13),
+                                    ((-1.1, 1.3), 1000), ((99.5, 100.5), 64),
+                                    ((0.0, 2.0), 4096)])
+def test_fp32_fast_bin_vote(cuts, S):
+    """Uniform-bin tables pass the kernels' uniformity vote (so the
+    table-free lookup is used for them); the edge tables of uniform-charge
+    slicing (order statistics of z) fail it and keep the exact search."""
+    from pyheadtail_gb300 import _engine as E
+    tail, head = cuts
+    e, neg = E.exact_edges(tail, (head - tail) / float(S), S, 1)
+    _, _, mg = _fast_bin_f32(e, e)
+    if mg < 0.25:
+        assert _edges_uniform_f32(e, mg)
+    rng = np.random.RandomState(S)
+    ce = np.sort(rng.normal(0, 0.23, S + 1)).astype(np.float32)
+    _, _, cmg = _fast_bin_f32(ce, ce)
+    assert cmg >= 0.25 or not _edges_uniform_f32(ce, cmg)
