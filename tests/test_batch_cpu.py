@@ -1,11 +1,13 @@
 """Host logic of the batched form (no GPU): bunch offsets, the unit plan
 that drives the persistent launch, the autotuner cache, and the host-side
-validation of the batched C entry points."""
+validation of the batched C entry points, the batch storage and its
+view check."""
 import ctypes
 import os
 
 import numpy as np
 import pytest
+import torch
 
 from pyheadtail_gb300 import _native as N
 from pyheadtail_gb300 import batch as B
@@ -117,3 +119,48 @@ def test_batch_entry_points_validate_on_host():
                                 None) == -1
     assert L.phk_batch_max_grid(7, 256, 100, 2) == -4
     assert L.phk_batch_max_grid(0, 96, 100, 2) == -4
+
+
+class _Engine(object):
+    z_version = 0
+
+    def flush(self):
+        pass
+
+
+class _Bunch(object):
+    """The parts of Particles a BunchBatch touches, on CPU tensors."""
+
+    def __init__(self, n, seed):
+        g = torch.Generator().manual_seed(seed)
+        self._c = {q: torch.randn(n, generator=g, dtype=torch.float64)
+                   for q in ('x', 'xp', 'y', 'yp', 'z', 'dp')}
+        self._code = N.PHK_F64
+        self._device = torch.device('cpu')
+        self._engine = _Engine()
+        self.macroparticlenumber = n
+        self._rebinds = 0
+
+
+def test_batch_views_and_rebind_check():
+    """A batch copies every bunch into one aligned storage and rebinds the
+    bunches' arrays to views of it; check_views looks again only when a
+    bunch's array was replaced (Particles counts that in _rebinds) and
+    raises if it no longer lives in the batch."""
+    from pyheadtail_gb300.batch import BunchBatch
+    bunches = [_Bunch(n, i) for i, n in enumerate((1000, 37, 4096))]
+    want = {id(b): {q: t.clone() for q, t in b._c.items()} for b in bunches}
+    batch = BunchBatch(bunches)
+    for b in bunches:
+        for q, t in b._c.items():
+            assert torch.equal(t, want[id(b)][q])
+            o = int(batch.offsets[bunches.index(b)])
+            assert t.data_ptr() == batch.storage[q][o:].data_ptr()
+    batch.check_views()
+    assert batch._rebinds_seen == [0, 0, 0]
+    batch.check_views()                      # unchanged: no second look
+    b = bunches[1]
+    b._c['xp'] = b._c['xp'].clone()          # what Particles._set does
+    b._rebinds += 1
+    with pytest.raises(RuntimeError, match='bunch 1: coordinate xp'):
+        batch.check_views()
