@@ -457,75 +457,75 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
                                               Tile<float, VEC>& t) {
     if constexpr (VEC == 2) {
         op_transverse_x2<OP0>(op, prog, t);
-        return;
-    }
-    const float* p = reinterpret_cast<const float*>(op.p);
-    const bool disp = op.flags & PHK_FLAG_DISPERSION;
-    const float Dx0 = p[32], Dx1 = p[33], Dy0 = p[34], Dy1 = p[35];
-    float (&x)[VEC] = t.c[PHK_X];
-    float (&xp)[VEC] = t.c[PHK_XP];
-    float (&y)[VEC] = t.c[PHK_Y];
-    float (&yp)[VEC] = t.c[PHK_YP];
-    const float (&dp)[VEC] = t.c[PHK_DP];
-    float M[8][VEC];
-    if (op.flags & PHK_FLAG_DETUNED) {
-        float dqx[VEC], dqy[VEC];
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) { dqx[j] = 0.f; dqy[j] = 0.f; }
-        const int nd = op.det_count;
-        if (OP0) {
-            if (nd > 0) detune_f32<VEC>(prog.det[0], t, dqx, dqy);
-            if (nd > 1) detune_f32<VEC>(prog.det[1], t, dqx, dqy);
-            for (int d = 2; d < nd; ++d) detune_f32<VEC>(prog.det[d], t, dqx, dqy);
-        } else {
-            for (int d = 0; d < nd; ++d)
-                detune_f32<VEC>(prog.det[op.det_begin + d], t, dqx, dqy);
-        }
-        const float qxh = p[16], qxl = p[17], qyh = p[18], qyl = p[19];
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) {
-            float sx, cx, sy, cy;
-            sincos_turns(qxh, qxl, dqx[j], &sx, &cx);
-            sincos_turns(qyh, qyl, dqy[j], &sy, &cy);
-            // I and J are float-float (p[40..55] their low parts)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                M[e][j] = fmaf(p[e], cx, fmaf(p[8 + e], sx,
-                                              fmaf(p[40 + e], cx, p[48 + e] * sx)));
-                M[4 + e][j] = fmaf(p[4 + e], cy,
-                                   fmaf(p[12 + e], sy,
-                                        fmaf(p[44 + e], cy, p[52 + e] * sy)));
-            }
-        }
     } else {
-#pragma unroll
-        for (int j = 0; j < VEC; ++j)
-#pragma unroll
-            for (int e = 0; e < 8; ++e) M[e][j] = p[e];
-    }
-    // low parts of a constant matrix (zero for a per-particle one)
-    const bool ml = !(op.flags & PHK_FLAG_DETUNED);
-#pragma unroll
-    for (int j = 0; j < VEC; ++j) {
-        if (disp) {
-            x[j] = fmaf(-Dx0, dp[j], x[j]);
-            y[j] = fmaf(-Dy0, dp[j], y[j]);
+        const float* p = reinterpret_cast<const float*>(op.p);
+        const bool disp = op.flags & PHK_FLAG_DISPERSION;
+        const float Dx0 = p[32], Dx1 = p[33], Dy0 = p[34], Dy1 = p[35];
+        float (&x)[VEC] = t.c[PHK_X];
+        float (&xp)[VEC] = t.c[PHK_XP];
+        float (&y)[VEC] = t.c[PHK_Y];
+        float (&yp)[VEC] = t.c[PHK_YP];
+        const float (&dp)[VEC] = t.c[PHK_DP];
+        float M[8][VEC];
+        if (op.flags & PHK_FLAG_DETUNED) {
+            float dqx[VEC], dqy[VEC];
+    #pragma unroll
+            for (int j = 0; j < VEC; ++j) { dqx[j] = 0.f; dqy[j] = 0.f; }
+            const int nd = op.det_count;
+            if (OP0) {
+                if (nd > 0) detune_f32<VEC>(prog.det[0], t, dqx, dqy);
+                if (nd > 1) detune_f32<VEC>(prog.det[1], t, dqx, dqy);
+                for (int d = 2; d < nd; ++d) detune_f32<VEC>(prog.det[d], t, dqx, dqy);
+            } else {
+                for (int d = 0; d < nd; ++d)
+                    detune_f32<VEC>(prog.det[op.det_begin + d], t, dqx, dqy);
+            }
+            const float qxh = p[16], qxl = p[17], qyh = p[18], qyl = p[19];
+    #pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                float sx, cx, sy, cy;
+                sincos_turns(qxh, qxl, dqx[j], &sx, &cx);
+                sincos_turns(qyh, qyl, dqy[j], &sy, &cy);
+                // I and J are float-float (p[40..55] their low parts)
+    #pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    M[e][j] = fmaf(p[e], cx, fmaf(p[8 + e], sx,
+                                                  fmaf(p[40 + e], cx, p[48 + e] * sx)));
+                    M[4 + e][j] = fmaf(p[4 + e], cy,
+                                       fmaf(p[12 + e], sy,
+                                            fmaf(p[44 + e], cy, p[52 + e] * sy)));
+                }
+            }
+        } else {
+    #pragma unroll
+            for (int j = 0; j < VEC; ++j)
+    #pragma unroll
+                for (int e = 0; e < 8; ++e) M[e][j] = p[e];
         }
-        float cxr = 0.f, cxp = 0.f, cyr = 0.f, cyp = 0.f;
-        if (ml) {
-            cxr = fmaf(p[40], x[j], p[41] * xp[j]);
-            cxp = fmaf(p[42], x[j], p[43] * xp[j]);
-            cyr = fmaf(p[44], y[j], p[45] * yp[j]);
-            cyp = fmaf(p[46], y[j], p[47] * yp[j]);
-        }
-        const float nx = fmaf(M[0][j], x[j], fmaf(M[1][j], xp[j], cxr));
-        const float nxp = fmaf(M[2][j], x[j], fmaf(M[3][j], xp[j], cxp));
-        const float ny = fmaf(M[4][j], y[j], fmaf(M[5][j], yp[j], cyr));
-        const float nyp = fmaf(M[6][j], y[j], fmaf(M[7][j], yp[j], cyp));
-        x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
-        if (disp) {
-            x[j] = fmaf(Dx1, dp[j], x[j]);
-            y[j] = fmaf(Dy1, dp[j], y[j]);
+        // low parts of a constant matrix (zero for a per-particle one)
+        const bool ml = !(op.flags & PHK_FLAG_DETUNED);
+    #pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            if (disp) {
+                x[j] = fmaf(-Dx0, dp[j], x[j]);
+                y[j] = fmaf(-Dy0, dp[j], y[j]);
+            }
+            float cxr = 0.f, cxp = 0.f, cyr = 0.f, cyp = 0.f;
+            if (ml) {
+                cxr = fmaf(p[40], x[j], p[41] * xp[j]);
+                cxp = fmaf(p[42], x[j], p[43] * xp[j]);
+                cyr = fmaf(p[44], y[j], p[45] * yp[j]);
+                cyp = fmaf(p[46], y[j], p[47] * yp[j]);
+            }
+            const float nx = fmaf(M[0][j], x[j], fmaf(M[1][j], xp[j], cxr));
+            const float nxp = fmaf(M[2][j], x[j], fmaf(M[3][j], xp[j], cxp));
+            const float ny = fmaf(M[4][j], y[j], fmaf(M[5][j], yp[j], cyr));
+            const float nyp = fmaf(M[6][j], y[j], fmaf(M[7][j], yp[j], cyp));
+            x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
+            if (disp) {
+                x[j] = fmaf(Dx1, dp[j], x[j]);
+                y[j] = fmaf(Dy1, dp[j], y[j]);
+            }
         }
     }
 }
@@ -543,15 +543,15 @@ __device__ __forceinline__ void op_drift(const phk_op& op,
         const float2 zs = shrink ? fma2(f2(br), Z, mul2(f2(brl), Z)) : Z;
         const float2 zn = fma2(f2(-etaL), DP, fma2(f2(-etaLl), DP, zs));
         t.c[PHK_Z][0] = zn.x; t.c[PHK_Z][1] = zn.y;
-        return;
-    }
-#pragma unroll
-    for (int j = 0; j < VEC; ++j) {
-        // z = beta_ratio * z - (eta0 * L) * dp, constants float-float
-        const float z = t.c[PHK_Z][j];
-        const float dp = t.c[PHK_DP][j];
-        const float zs = shrink ? fmaf(br, z, brl * z) : z;
-        t.c[PHK_Z][j] = fmaf(-etaL, dp, fmaf(-etaLl, dp, zs));
+    } else {
+    #pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            // z = beta_ratio * z - (eta0 * L) * dp, constants float-float
+            const float z = t.c[PHK_Z][j];
+            const float dp = t.c[PHK_DP][j];
+            const float zs = shrink ? fmaf(br, z, brl * z) : z;
+            t.c[PHK_Z][j] = fmaf(-etaL, dp, fmaf(-etaLl, dp, zs));
+        }
     }
 }
 
@@ -585,20 +585,20 @@ __device__ __forceinline__ void op_rfkick(const phk_op& op,
         t.c[PHK_DP][0] = DP.x; t.c[PHK_DP][1] = DP.y;
         t.c[PHK_X][0] = X.x; t.c[PHK_X][1] = X.y;
         t.c[PHK_Y][0] = Y.x; t.c[PHK_Y][1] = Y.y;
-        return;
-    }
-#pragma unroll
-    for (int j = 0; j < VEC; ++j) {
-        float& dp = t.c[PHK_DP][j];
-        if (disp) {
-            t.c[PHK_X][j] = fmaf(-Dx, dp, t.c[PHK_X][j]);
-            t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
-        }
-        const float s = sin_turns_of_product(t.c[PHK_Z][j], mh, ml, oh, ol);
-        dp = fmaf(A, s, fmaf(Al, s, fmaf(dp, ratio, fmaf(dp, ratiol, -pinc))));
-        if (disp) {
-            t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
-            t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);
+    } else {
+    #pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            float& dp = t.c[PHK_DP][j];
+            if (disp) {
+                t.c[PHK_X][j] = fmaf(-Dx, dp, t.c[PHK_X][j]);
+                t.c[PHK_Y][j] = fmaf(-Dy, dp, t.c[PHK_Y][j]);
+            }
+            const float s = sin_turns_of_product(t.c[PHK_Z][j], mh, ml, oh, ol);
+            dp = fmaf(A, s, fmaf(Al, s, fmaf(dp, ratio, fmaf(dp, ratiol, -pinc))));
+            if (disp) {
+                t.c[PHK_X][j] = fmaf(Dx, dp, t.c[PHK_X][j]);
+                t.c[PHK_Y][j] = fmaf(Dy, dp, t.c[PHK_Y][j]);
+            }
         }
     }
 }
