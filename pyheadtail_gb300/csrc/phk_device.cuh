@@ -268,9 +268,11 @@ __device__ __forceinline__ float sin_turns_of_product(float z, float mh,
 
 // ------------------------------------------- packed FP32 pairs (f32x2)
 // Two particles per instruction on the sm_100 family's paired FP32 pipes
-// (FFMA2 / FADD2 / FMUL2).  Each lane is rounded exactly as the scalar
-// fmaf / + / * it stands for, so the packed forms below return, lane for
-// lane, the bits of their scalar counterparts above.
+// (FFMA2 / FADD2 / FMUL2).  Each lane rounds as an IEEE fmaf / + / * and
+// the packed operations are never contracted, so the forms below run the
+// operation sequence of their scalar counterparts above, lane by lane,
+// with every written rounding kept (the scalar forms leave the compiler
+// free to fuse a product into a following sum).
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
