@@ -15,10 +15,11 @@ it can only be produced while the beam's z is still the one the SliceSet
 was made from (SliceSets describe a past state), otherwise it raises.
 """
 from abc import ABCMeta, abstractmethod
-from functools import wraps
+from functools import partial, wraps
 
 import numpy as np
 import torch
+from scipy import interpolate, ndimage
 from scipy.constants import c, e
 
 from .. import _engine as E
@@ -36,8 +37,19 @@ def clean_slices(long_track_method):
     return cleaned
 
 
+def make_int32(array):
+    """slicing.py:29-30."""
+    return array.astype(np.int32)
+
+
 class ModeIsUniformCharge(Exception):
-    pass
+    """slicing.py:33-37."""
+
+    def __init__(self, message):
+        self.message = message
+
+    def __str__(self):
+        return self.message
 
 
 class SliceSet(Printing):
@@ -54,6 +66,7 @@ class SliceSet(Printing):
         self._z_version = beam._engine.z_version
         self._slice_index_of_particle = None
         self._particles_within_cuts = None
+        self._particle_indices_by_slice = None
         for k, v in beam_parameters.items():
             if hasattr(self, k):
                 raise ValueError('SliceSet.' + k + ' already exists!')
@@ -74,6 +87,11 @@ class SliceSet(Printing):
     @property
     def n_slices(self):
         return len(self.z_bins) - 1
+
+    @property
+    def smoothing_sigma(self):
+        """slicing.py:133-134."""
+        return 0.02 * self.n_slices
 
     @property
     def slice_widths(self):
@@ -126,9 +144,96 @@ class SliceSet(Printing):
         pos[1:] = torch.cumsum(self.n_macroparticles_per_slice, 0)
         return pos
 
+    @property
+    def particles_within_cuts_slice(self):
+        """slicing.py:187-197.  The particles are never reordered by the
+        slicing here (is_sorted is False), so this is particles_within_cuts
+        as on the reference's CPU path."""
+        if getattr(self, 'is_sorted', False):
+            return slice(self.pidx_begin, self.pidx_end, 1)
+        return self.particles_within_cuts
+
+    @property
+    def pidx_begin(self):
+        """Index of the first particle within the cuts (slicing.py:199-204)."""
+        return int(self.particles_within_cuts[0])
+
+    @property
+    def pidx_end(self):
+        """Index after the last particle within the cuts (:206-211)."""
+        return int(self.particles_within_cuts[-1]) + 1
+
+    @property
+    def particle_indices_by_slice(self):
+        """Particle indices within the cuts grouped by slice, ascending
+        inside a slice (the counting sort of slicing.py:214-227): a stable
+        sort of particles_within_cuts by slice index."""
+        if self._particle_indices_by_slice is None:
+            p = self.particles_within_cuts
+            s = self.slice_index_of_particle[p.long()]
+            order = torch.sort(s, stable=True)[1]
+            self._particle_indices_by_slice = p[order]
+        return self._particle_indices_by_slice
+
     def particle_indices_of_slice(self, slice_index):
         p = self.particles_within_cuts
         return p[self.slice_index_of_particle[p] == slice_index]
+
+    # -- line density (slicing.py:229-292), on the host from the counts
+    def _counts_host(self):
+        n = self.n_macroparticles_per_slice
+        n = n.cpu().numpy() if torch.is_tensor(n) else np.asarray(n)
+        return n.astype(np.int32)
+
+    def lambda_bins(self, sigma=None, smoothen=True):
+        """Line charge density per bin (slicing.py:229-237)."""
+        if sigma is None:
+            sigma = self.smoothing_sigma
+        lambda_of_bins = self._counts_host() * self.charge_per_mp
+        if smoothen:
+            lambda_of_bins = ndimage.gaussian_filter1d(
+                lambda_of_bins, sigma=sigma, mode='nearest')
+        return lambda_of_bins
+
+    def lambda_prime_bins(self, sigma=None, smoothen_before=True,
+                          smoothen_after=True):
+        """Derivative of the line charge density per bin, Gaussian-smoothed
+        (slicing.py:239-268); the smoothing before the gradient acts on the
+        int32 counts, as the reference's does."""
+        if self.mode == 'uniform_charge':
+            raise ModeIsUniformCharge('The derivative is zero up to '
+                                      'numerical fluctuations because the '
+                                      'charges have been distributed '
+                                      'uniformly across the slices.')
+        if sigma is None:
+            sigma = self.smoothing_sigma
+        smoothen = partial(ndimage.gaussian_filter1d, sigma=sigma,
+                           mode='nearest')
+        line_density = self._counts_host()
+        if smoothen_before:
+            line_density = smoothen(line_density)
+        mp_density_derivative = np.gradient(line_density,
+                                            self.slice_widths[0])
+        if smoothen_after:
+            mp_density_derivative = smoothen(mp_density_derivative)
+        return mp_density_derivative * self.charge_per_mp
+
+    def lambda_z(self, z=None, sigma=None, smoothen=True):
+        """Line charge density along z (slicing.py:270-281)."""
+        lambda_along_bins = (self.lambda_bins(sigma, smoothen)
+                             / self.slice_widths)
+        if z is None:
+            return lambda_along_bins
+        tck = interpolate.splrep(self.z_centers, lambda_along_bins, s=0)
+        return interpolate.splev(z, tck, der=0, ext=1)
+
+    def lambda_prime_z(self, z, sigma=None, smoothen_before=True,
+                       smoothen_after=True):
+        """Derivative of the line charge density along z (:283-292)."""
+        lp_along_bins = self.lambda_prime_bins(
+            sigma, smoothen_before, smoothen_after) / self.slice_widths
+        tck = interpolate.splrep(self.z_centers, lp_along_bins, s=0)
+        return interpolate.splev(z, tck, der=0, ext=1)
 
     def convert_to_time(self, z):
         """slicing.py:303-307."""
@@ -184,6 +289,20 @@ class Slicer(Printing, metaclass=ABCMeta):
                     particlenumber_per_mp=beam.particlenumber_per_mp,
                     charge=beam.charge, charge_per_mp=beam.charge_per_mp,
                     mass=beam.mass, intensity=beam.intensity)
+
+    def update_slices(self, beam):
+        """Removed from the reference's interface (slicing.py:428-436)."""
+        raise RuntimeError('update_slices(beam) no longer exists. '
+                           'Instead, remove all previously recorded SliceSet'
+                           'objects in the beam via beam.clean_slices() '
+                           'when the longitudinal state of the beam is '
+                           'changed. Concretely: replace '
+                           'slices.update_slices(beam) by '
+                           'beam.clean_slices().The SliceSet objects should '
+                           'be retrieved via beam.get_slices(Slicer) '
+                           '*only*. In this way the beam can memorize '
+                           'previously created slice snapshots. This '
+                           'minimises computation time.')
 
     def get_long_cuts(self, beam):
         """slicing.py:395-413."""
