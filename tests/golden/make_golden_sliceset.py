@@ -5,7 +5,8 @@ lambda_prime_z), made by running PyHEADTAIL itself on a seeded bunch:
 
     python tests/golden/make_golden_sliceset.py [--ref /root/reference]
 
-Writes tests/golden/sliceset_analysis.npz: the slicing (z_bins, slice index
+Writes tests/golden/sliceset/analysis.npz (a subdirectory, apart from
+the turn-loop fixtures that the parity tests collect): the slicing (z_bins, slice index
 of every particle, counts, charge per macroparticle) and every method's
 output, for a uniform-bin and a uniform-charge slicing.
 """
@@ -63,7 +64,7 @@ def main():
         except ModeIsUniformCharge:
             out[p + 'lambda_prime_raises'] = np.bool_(True)
     out['zq'] = zq
-    path = os.path.join(HERE, 'sliceset_analysis.npz')
+    path = os.path.join(HERE, 'sliceset', 'analysis.npz')
     np.savez_compressed(path, **out)
     print('wrote', path, len(out), 'arrays')
 

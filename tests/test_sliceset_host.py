@@ -1,5 +1,5 @@
 """SliceSet's analysis methods on the host (no GPU), against the
-reference's own values (tests/golden/sliceset_analysis.npz, made by
+reference's own values (tests/golden/sliceset/analysis.npz, made by
 make_golden_sliceset.py running PyHEADTAIL): smoothing_sigma,
 particle_indices_by_slice, pidx_begin / pidx_end,
 particles_within_cuts_slice, lambda_bins, lambda_prime_bins, lambda_z,
@@ -39,7 +39,7 @@ def _sliceset(g, tag):
 
 @pytest.fixture(scope='module')
 def golden():
-    with np.load(os.path.join(GOLDEN, 'sliceset_analysis.npz')) as f:
+    with np.load(os.path.join(GOLDEN, 'sliceset', 'analysis.npz')) as f:
         return {k: f[k] for k in f.files}
 
 
