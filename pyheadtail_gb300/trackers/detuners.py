@@ -40,14 +40,49 @@ class ChromaticitySegment(SegmentDetuner):
             raise ValueError('chromaticity orders above %d are not supported'
                              % N.PHK_MAX_POLY)
         # the reference's polyval path (order > 3) prepends one zero
-        # coefficient per call (detuners.py:95-97): count the calls
-        self._calls = 0
+        # coefficient per call (detuners.py:95-97): count the calls per
+        # plane; the kernel and calc_detuning_x / _y read the same counts
+        self._calls = [0, 0]
+        self.calc_detuning_x = self._plane_detuning(0)
+        self.calc_detuning_y = self._plane_detuning(1)
 
-    def _extra(self, coeffs):
-        return self._calls - 1 if len(coeffs) > 3 else 0
+    def _coeffs(self, q):
+        return self.coeffs_x if q == 0 else self.coeffs_y
+
+    def _bump(self, q):
+        if len(self._coeffs(q)) > 3:
+            self._calls[q] += 1
+
+    def _extra_of(self, q):
+        return max(self._calls[q] - 1, 0) if len(self._coeffs(q)) > 3 else 0
+
+    def _plane_detuning(self, q):
+        def calc_detuning(dp):
+            """The plane's detuning of an array dp (numpy or torch):
+            ChromaticitySegment.calc_detuning_x / _y (detuners.py:74-98)."""
+            self._bump(q)
+            return _chroma_poly(self._coeffs(q), self._extra_of(q), dp)
+        return calc_detuning
+
+    @staticmethod
+    def _make_calc_detuning(Qp):
+        """A stand-alone detuning polynomial of the chromaticities Qp
+        (detuners.py:74-98): orders 1-3 written out, higher orders with
+        the reference's zero prepended on every call."""
+        coeffs = [Qp[i] / float(factorial(i + 1)) for i in range(len(Qp))]
+        calls = [0]
+
+        def calc_detuning(dp):
+            extra = 0
+            if len(coeffs) > 3:
+                calls[0] += 1
+                extra = calls[0] - 1
+            return _chroma_poly(coeffs, extra, dp)
+        return calc_detuning
 
     def _pack(self, beam):
-        self._calls += 1
+        self._bump(0)
+        self._bump(1)
         c = {}
         cf = {}
         for i, v in enumerate(self.coeffs_x):
@@ -58,18 +93,30 @@ class ChromaticitySegment(SegmentDetuner):
             cf[8 + i] = np.float32(v)
         return E.DetunerPack(N.DET_CHROMA, c, cf, nx=len(self.coeffs_x),
                              ny=len(self.coeffs_y),
-                             zx=self._extra(self.coeffs_x),
-                             zy=self._extra(self.coeffs_y))
+                             zx=self._extra_of(0), zy=self._extra_of(1))
 
     def detune(self, beam):
+        """detuners.py:64-69 (device tensors; the fused kernel evaluates
+        the same polynomials in the track pass)."""
         dp = beam.dp.double()
+        return self.calc_detuning_x(dp), self.calc_detuning_y(dp)
 
-        def poly(cs):
-            r = cs[-1] * 1.0 + 0 * dp
-            for cc in cs[-2::-1]:
-                r = cc + r * dp
-            return r * dp
-        return poly(self.coeffs_x), poly(self.coeffs_y)
+
+def _chroma_poly(coeffs, extra, dp):
+    """(c0 + (c1 + ...) dp) dp times dp**extra: the reference's explicit
+    orders 1-3 and, above, np.polynomial.polynomial.polyval over the
+    coefficients with 1 + extra zeros prepended (Horner: the zeros only
+    multiply by dp, exactly)."""
+    if len(coeffs) == 1:
+        r = coeffs[0] * dp
+    else:
+        r = coeffs[-1] + 0 * dp
+        for cc in coeffs[-2::-1]:
+            r = cc + r * dp
+        r = r * dp
+    for _ in range(extra):
+        r = r * dp
+    return r
 
 
 class AmplitudeDetuningSegment(SegmentDetuner):

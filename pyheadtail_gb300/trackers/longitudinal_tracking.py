@@ -273,6 +273,67 @@ class RFSystems(LongitudinalOneTurnMap):
     def track_transverse_shrinking(self, beam):
         self.track(beam)
 
+    def track_no_transverse_shrinking(self, beam):
+        """The RF elements only, without the transverse adiabatic damping
+        (longitudinal_tracking.py:576-580)."""
+        for m in self._elements:
+            m.track(beam)
+        if self.p_increment:
+            self.clean_buckets()
+        beam.clean_slices()
+
+    def clean_buckets(self):
+        """longitudinal_tracking.py:525-530; no RFBucket is kept here, so
+        there is nothing else to erase."""
+        self._rfbuckets = {}
+
+    # -- removed from the reference's interface: the same notices
+    #    (longitudinal_tracking.py:595-648)
+    @property
+    def rfbucket(self):
+        raise RuntimeError('Interface change: ' +
+                           'Use the get_bucket(beam) method ' +
+                           'to obtain a (constant) blueprint of the ' +
+                           'current state of the ' +
+                           'longitudinal RF configuration.')
+
+    @property
+    def kicks(self):
+        raise RuntimeError('Interface change: ' +
+                           'Use the voltages, harmonics or phi_offsets ' +
+                           'lists of RFSystems to access the kick parameters.')
+
+    @property
+    def elements(self):
+        raise RuntimeError('Interface change: ' +
+                           'Use the voltages, harmonics or phi_offsets ' +
+                           'lists of RFSystems to access the kick parameters.')
+
+    @property
+    def fundamental_kick(self):
+        raise RuntimeError('Interface change: ' +
+                           'Use the voltages, harmonics or phi_offsets ' +
+                           'lists of RFSystems to access the kick parameters.')
+
+    @property
+    def accelerating_kick(self):
+        raise RuntimeError('Interface change: ' +
+                           'Use the first entries of the voltages, harmonics ' +
+                           'or phi_offsets lists of RFSystems to access the ' +
+                           'kick parameters.')
+
+    def set_voltage_list(self, voltage_list):
+        raise RuntimeError('Interface change: ' +
+                           'Use the list RFSystems.voltages .')
+
+    def set_harmonic_list(self, harmonic_list):
+        raise RuntimeError('Interface change: ' +
+                           'Use the list RFSystems.harmonics .')
+
+    def set_phi_offset_list(self, phi_offset_list):
+        raise RuntimeError('Interface change: ' +
+                           'Use the list RFSystems.phi_offsets .')
+
     @property
     def Q_s(self):
         """Small-amplitude synchrotron tune of this RF system at its
@@ -307,6 +368,11 @@ class LinearMap(LongitudinalOneTurnMap):
         if len(alpha_array) > 1:
             self.warns('The higher orders in the given alpha_array are '
                        'manifestly neglected.')
+
+    @property
+    def Qs(self):
+        """longitudinal_tracking.py:716-718."""
+        return self.Q_s
 
     def _op(self, beam):
         omega_0 = 2 * np.pi * beam.beta * c / self.circumference
