@@ -221,6 +221,70 @@ class Particles(Printing):
     def clean_slices(self):
         self._slice_sets = {}
 
+    def _empty_like(self, macroparticlenumber):
+        """A beam with this one's scalars, precision and device and no
+        coordinates yet."""
+        return Particles(macroparticlenumber, self.particlenumber_per_mp,
+                         self.charge, self.mass, self.circumference,
+                         self.gamma, coords_n_momenta_dict={},
+                         precision=self.precision, device=self._device)
+
+    def extract_slices(self, slicer, include_non_sliced='if_any', *args,
+                       **kwargs):
+        """One Particles per slice, plus one of the particles outside the
+        cuts (particles/particles.py:150-207), each with ``slice_info``."""
+        if include_non_sliced not in ['if_any', 'always', 'never']:
+            raise ValueError("include_non_sliced=%s is not valid!\n"
+                             % include_non_sliced +
+                             "Possible values are {'always', 'never', "
+                             "'if_any'}")
+        slices = self.get_slices(slicer, *args, **kwargs)
+        _ = slices.slice_index_of_particle  # taken while z is the sliced one
+        coords = self.get_coords_n_momenta_dict()
+        out = []
+        for i_sl in range(slices.n_slices):
+            ix = slices.particle_indices_of_slice(i_sl).long()
+            so = self._empty_like(len(ix))
+            so.update({k: v[ix] for k, v in coords.items()})
+            so.id[:] = self.id[ix]
+            so.slice_info = {'z_bin_center': slices.z_centers[i_sl],
+                             'z_bin_right': slices.z_bins[i_sl + 1],
+                             'z_bin_left': slices.z_bins[i_sl]}
+            out.append(so)
+        if include_non_sliced != 'never':
+            ix = slices.particles_outside_cuts.long()
+            if len(ix) > 0 or include_non_sliced == 'always':
+                so = self._empty_like(len(ix))
+                so.update({k: v[ix] for k, v in coords.items()})
+                so.id[:] = self.id[ix]
+                so.slice_info = 'unsliced'
+                out.append(so)
+        return out
+
+    def __add__(self, other):
+        """Merges two beams: coordinates and ids concatenated, the scalars
+        of the left one (particles/particles.py:264-288)."""
+        a = self.get_coords_n_momenta_dict()
+        b = other.get_coords_n_momenta_dict()
+        result = self._empty_like(self.macroparticlenumber +
+                                  other.macroparticlenumber)
+        result.update({k: torch.cat((a[k], b[k].to(device=a[k].device,
+                                                     dtype=a[k].dtype)))
+                       for k in a})
+        result.id = torch.cat((self.id, other.id.to(self.id.device)))
+        return result
+
+    def __radd__(self, other):
+        """``0 + beam`` is a copy of the beam (so that sum() works),
+        anything else merges (particles/particles.py:290-305)."""
+        if other == 0:
+            result = self._empty_like(self.macroparticlenumber)
+            result.update({k: v.clone() for k, v in
+                           self.get_coords_n_momenta_dict().items()})
+            result.id = self.id.clone()
+            return result
+        return self.__add__(other)
+
     # -------------------------------------------------- statistics
     # Every statistic is derived from one phk_bunch_stats record of the
     # current state: one read-only pass over the coordinates, with the
