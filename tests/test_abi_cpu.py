@@ -251,3 +251,37 @@ def test_fp32_fast_bin_vote(cuts, S):
     ce = np.sort(rng.normal(0, 0.23, S + 1)).astype(np.float32)
     _, _, cmg = _fast_bin_f32(ce, ce)
     assert cmg >= 0.25 or not _edges_uniform_f32(ce, cmg)
+
+
+def test_fp32_fast_bin_path_random_slicers():
+    """The table-free path's margin over 60 seeded random uniform slicers
+    (cuts anywhere in [-5, 5], spans 1e-4 .. 10, 1 .. 4096 slices, either
+    orientation): wherever it is taken, on every edge and 4 neighbours
+    either side and on random z, it gives the reference's index."""
+    from pyheadtail_gb300 import _engine as E
+    rng = np.random.RandomState(2024)
+    taken = 0
+    for _ in range(60):
+        S = int(rng.choice([1, 2, 7, 50, 100, 500, 1000, 4096]))
+        span = 10.0 ** rng.uniform(-4, 1)
+        tail = rng.uniform(-5, 5)
+        head = tail + span * (1 if rng.rand() < 0.8 else -1)
+        width = (head - tail) / float(S)
+        e, neg = E.exact_edges(tail, width, S, 1)
+        ez = (-e if neg else e).astype(np.float32)
+        near = [ez]
+        lo, hi = ez.copy(), ez.copy()
+        for _ in range(4):
+            lo = np.nextafter(lo, np.float32(-np.inf))
+            hi = np.nextafter(hi, np.float32(np.inf))
+            near += [lo, hi]
+        z = np.concatenate(near + [rng.uniform(min(tail, head) - 0.1 * span,
+                                               max(tail, head) + 0.1 * span,
+                                               20000).astype(np.float32)])
+        want = np.floor((z.astype(np.float64) - tail) / width)
+        k, ok, mg = _fast_bin_f32(-z if neg else z, e)
+        if mg < 0.25:
+            assert _edges_uniform_f32(e, mg), (tail, head, S)
+        assert np.array_equal(k[ok], want[ok].astype(np.int64)), (tail, head, S)
+        taken += int(ok.sum())
+    assert taken > 0
