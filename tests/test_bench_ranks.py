@@ -44,3 +44,32 @@ def test_single_rank_needs_no_process_group():
     import bench
     assert bench.max_over_ranks(3.25, 1) == 3.25
     assert bench.job_value(500, 2.0, 1) == pytest.approx(2.5e5)
+
+
+def test_reference_arm_line_keeps_the_contract():
+    """bench.py --impl reference on the host: one JSON line with the arm's
+    metric, a cpu_baseline describing the run and an e2e equal to it with
+    no host-device bytes; rank 1 of a 2-rank launch prints nothing."""
+    import json
+    import subprocess
+    cmd = [sys.executable, os.path.join(ROOT, 'bench.py'), '--impl',
+           'reference', '--steps', '3', '--warmup', '3']
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600,
+                         cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith('{')]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d['impl'] == 'reference'
+    assert d['unit'] == 'macroparticle-turns/s' and d['higher_is_better']
+    assert d['value'] > 0 and d['steps'] == 3 and d['warmup'] == 3
+    cb = d['cpu_baseline']
+    assert cb['value'] == d['value'] and cb['cores'] >= 1
+    assert cb['kind'] in ('port', 'reference') and cb['sample']
+    assert d['e2e'] == {'value': d['value'], 'unit': d['unit'],
+                        'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
+    env = dict(os.environ, WORLD_SIZE='2', RANK='1', LOCAL_RANK='1')
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600,
+                         cwd=ROOT, env=env)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert not [l for l in out.stdout.splitlines() if l.startswith('{')]
