@@ -63,10 +63,10 @@ class TransverseDamper(Element):
     def vertical(cls, dampingrate_y, *args, **kwargs):
         return cls(0, dampingrate_y, *args, **kwargs)
 
-    def _op(self, means):
+    def _op(self, means, gains):
         flags, p = 0, {}
         coords = ()
-        for pl, gain in ((0, self.gain_x), (1, self.gain_y)):
+        for pl, gain in ((0, gains[0]), (1, gains[1])):
             if gain is None:
                 continue
             flags |= N.FLAG_DAMP_X if pl == 0 else N.FLAG_DAMP_Y
@@ -87,9 +87,33 @@ class TransverseDamper(Element):
                      pointer=means.data_ptr()), S.mask_of(coords))
 
     def track(self, beam):
-        """transverse_damper.py:64-86 (track_horizontal / _vertical /
+        """transverse_damper.py:64-86: the planes whose damping rate is
+        set (the reference binds track to track_horizontal, _vertical or
         _all), deferred to the beam's next pass."""
-        if self.gain_x is None and self.gain_y is None:
+        self._track_planes(beam, (self.gain_x, self.gain_y))
+
+    def track_horizontal(self, beam):
+        """transverse_damper.py:68-72."""
+        self._track_planes(beam, (self._gain('x'), None))
+
+    def track_vertical(self, beam):
+        """transverse_damper.py:74-78."""
+        self._track_planes(beam, (None, self._gain('y')))
+
+    def track_all(self, beam):
+        """transverse_damper.py:80-88."""
+        self._track_planes(beam, (self._gain('x'), self._gain('y')))
+
+    def _gain(self, plane):
+        g = self.gain_x if plane == 'x' else self.gain_y
+        if g is None:
+            # the reference's arithmetic on an unset gain fails the same way
+            raise TypeError('TransverseDamper: no damping rate in the %s '
+                            'plane' % plane)
+        return g
+
+    def _track_planes(self, beam, gains):
+        if gains[0] is None and gains[1] is None:
             return
         buf = self._bufs.get(beam)
         if buf is None:
@@ -98,7 +122,7 @@ class TransverseDamper(Element):
                    torch.zeros(9, dtype=torch.float64, device=beam._device))
             self._bufs[beam] = buf
         rec, means = buf
-        op, mask = self._op(means)
+        op, mask = self._op(means, gains)
         op.keepalive = means        # referenced by pointer until the pass
         beam.launch_stats(rec, order=1, mask=mask, means=means)
         beam._engine.enqueue(op)
