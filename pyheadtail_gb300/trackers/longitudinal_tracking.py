@@ -90,13 +90,17 @@ class Kick(LongitudinalMap):
         self.D_x = D_x
         self.D_y = D_y
 
-    def _op(self, beam):
+    def _op(self, beam, dispersion=None):
+        """The RF_KICK op; dispersion: True / False force the reference's
+        track_with_dispersion / track_without_dispersion, None follows
+        D_x, D_y as its track does (longitudinal_tracking.py:168-181)."""
         amplitude = np.abs(beam.charge) * self.voltage / (beam.beta * c)
         p0_old = beam.p0
         beam.p0 += self.p_increment
         p0_new = beam.p0
         flags = 0
-        if self.D_x or self.D_y:
+        if (bool(self.D_x or self.D_y) if dispersion is None
+                else dispersion):
             flags |= N.FLAG_DISPERSION
         if self.phi_offset != 0:
             flags |= N.FLAG_PHI_OFFSET
@@ -127,8 +131,13 @@ class Kick(LongitudinalMap):
     def track(self, beam):
         beam._engine.enqueue(self._op(beam))
 
-    track_with_dispersion = track
-    track_without_dispersion = track
+    def track_with_dispersion(self, beam):
+        """longitudinal_tracking.py:183-193."""
+        beam._engine.enqueue(self._op(beam, dispersion=True))
+
+    def track_without_dispersion(self, beam):
+        """longitudinal_tracking.py:195-203."""
+        beam._engine.enqueue(self._op(beam, dispersion=False))
 
 
 class LongitudinalOneTurnMap(LongitudinalMap, metaclass=ABCMeta):
@@ -374,15 +383,18 @@ class LinearMap(LongitudinalOneTurnMap):
         """longitudinal_tracking.py:716-718."""
         return self.Q_s
 
-    def _op(self, beam):
+    def _op(self, beam, dispersion=None):
+        """The LINEAR_LONG op; dispersion as for Kick._op (D = 0 makes the
+        reference's dispersion passes, :731-741, no-ops)."""
         omega_0 = 2 * np.pi * beam.beta * c / self.circumference
         omega_s = self.Q_s * omega_0
         dQ_s = 2 * np.pi * self.Q_s
         cosdQ_s = np.cos(dQ_s)
         sindQ_s = np.sin(dQ_s)
         longfac = self.eta(0, beam.gamma) * beam.beta * c / omega_s
-        # D = 0 makes the reference's dispersion passes (:731-741) no-ops
-        flags = N.FLAG_DISPERSION if (self.D_x or self.D_y) else 0
+        flags = N.FLAG_DISPERSION if (
+            bool(self.D_x or self.D_y) if dispersion is None
+            else dispersion) else 0
         p = {0: float(cosdQ_s), 1: float(sindQ_s), 2: float(longfac),
              3: float(self.D_x), 4: float(self.D_y), 5: 1. / float(longfac)}
         # precision form: float-float cos, longfac*sin and sin/longfac
@@ -397,5 +409,12 @@ class LinearMap(LongitudinalOneTurnMap):
         beam._engine.enqueue(self._op(beam))
         beam.clean_slices()
 
-    track_with_dispersion = track
-    track_without_dispersion = track
+    def track_with_dispersion(self, beam):
+        """longitudinal_tracking.py:731-741."""
+        beam._engine.enqueue(self._op(beam, dispersion=True))
+        beam.clean_slices()
+
+    def track_without_dispersion(self, beam):
+        """longitudinal_tracking.py:743-759."""
+        beam._engine.enqueue(self._op(beam, dispersion=False))
+        beam.clean_slices()

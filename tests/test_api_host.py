@@ -4,10 +4,11 @@ _make_calc_detuning, detuners.py:48-98) against the oracle's restatement,
 including the reference's order > 3 behaviour (one more zero coefficient
 prepended on every call, detuners.py:95-97) and its agreement with what the
 kernel is told (_pack); RFSystems' removed-interface notices and
-clean_buckets (longitudinal_tracking.py:525-648); LinearMap.Qs (:716-718)."""
+clean_buckets (longitudinal_tracking.py:525-648); LinearMap.Qs (:716-718);
+the dispersion entry points of Kick and LinearMap (:183-203, :731-759)."""
 import numpy as np
 import pytest
-from scipy.constants import e, m_p
+from scipy.constants import c, e, m_p
 
 from oracle import turn_loop as T
 
@@ -76,3 +77,46 @@ def test_rfsystems_lists_and_buckets_still_work():
 def test_linear_map_qs():
     lm = LinearMap([1.8e-3], 6911.5, 0.017)
     assert lm.Qs == lm.Q_s == 0.017
+
+
+class _LongBeam(object):
+    """The beam scalars and engine that Kick / LinearMap ops read."""
+
+    def __init__(self):
+        self.charge, self.mass = e, m_p
+        self.gamma = 27.7
+        self.beta = np.sqrt(1 - self.gamma**-2)
+        self.p0 = np.sqrt(self.gamma**2 - 1) * m_p * c
+        self.ops = []
+        beam = self
+
+        class _Engine(object):
+            def enqueue(self, op):
+                beam.ops.append(op)
+        self._engine = _Engine()
+
+    def clean_slices(self):
+        pass
+
+
+@pytest.mark.parametrize('D', [0., 0.7])
+def test_dispersion_entry_points(D):
+    """track follows D_x, D_y (the reference binds track to one of the two);
+    track_with_dispersion / track_without_dispersion set or clear the
+    dispersion passes whatever D is, with all other parameters equal."""
+    from pyheadtail_gb300 import _native as N
+    from pyheadtail_gb300.trackers.longitudinal_tracking import Kick
+    for el in (Kick([1.8e-3], 6911.5, 4620, 4.5e6, D_x=D),
+               LinearMap([1.8e-3], 6911.5, 0.017, D_x=D)):
+        ops = {}
+        for m in ('track', 'track_with_dispersion', 'track_without_dispersion'):
+            b = _LongBeam()
+            getattr(el, m)(b)
+            ops[m] = b.ops[0]
+        disp = {m: bool(op.flags & N.FLAG_DISPERSION) for m, op in ops.items()}
+        assert disp == {'track': D != 0, 'track_with_dispersion': True,
+                        'track_without_dispersion': False}
+        for op in ops.values():
+            assert op.p == ops['track'].p and op.kind == ops['track'].kind
+            assert (op.flags | N.FLAG_DISPERSION) == \
+                (ops['track'].flags | N.FLAG_DISPERSION)
