@@ -322,6 +322,16 @@ class Slicer(Printing, metaclass=ABCMeta):
     def slice(self, beam, *args, **kwargs):
         pass
 
+    def compute_sliceset_kwargs(self, beam):
+        """The SliceSet arguments of the beam's current state
+        (slicing.py:340-346, 599-615, 636-686): z_bins, the slice index of
+        every particle, the mode and the counts per slice."""
+        ss = make_slice_set(self, beam)
+        return dict(z_bins=ss.z_bins,
+                    slice_index_of_particle=ss.slice_index_of_particle,
+                    mode=ss.mode,
+                    n_macroparticles_per_slice=ss.n_macroparticles_per_slice)
+
 
 class UniformBinSlicer(Slicer):
     """Uniform bins over the slicing region (slicing.py:532-615)."""

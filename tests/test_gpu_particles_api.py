@@ -75,3 +75,28 @@ def test_extract_slices():
     assert len(b.extract_slices(sl, include_non_sliced='always')) == S + 1
     with pytest.raises(ValueError):
         b.extract_slices(sl, include_non_sliced='sometimes')
+
+
+@pytest.mark.parametrize('mode', ['uniform_bin', 'uniform_charge'])
+def test_compute_sliceset_kwargs(mode):
+    """Slicer.compute_sliceset_kwargs gives the arguments of the SliceSet
+    that slice() makes from the same state."""
+    import cases as C
+    import gpu_cases as G
+    import random
+    b, c = _beam(3000, 6)
+    sl = G.make_slicer(C.slicer(30, mode=mode))
+    # uniform-charge slicing hands the remainder particles to random
+    # slices (the reference's random.sample): same seed for both
+    random.seed(11)
+    kw = sl.compute_sliceset_kwargs(b)
+    random.seed(11)
+    ss = sl.slice(b)
+    assert set(kw) == {'z_bins', 'slice_index_of_particle', 'mode',
+                       'n_macroparticles_per_slice'}
+    assert kw['mode'] == ss.mode == mode
+    np.testing.assert_array_equal(kw['z_bins'], ss.z_bins)
+    assert torch.equal(kw['slice_index_of_particle'],
+                       ss.slice_index_of_particle)
+    assert torch.equal(kw['n_macroparticles_per_slice'],
+                       ss.n_macroparticles_per_slice)
