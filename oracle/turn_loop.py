@@ -991,6 +991,24 @@ def circular_resistive_wall_kicks(slicer, pipe_radius, length, conductivity,
             WakeKick(wf, slicer, n_turns_wake, 'yp', 'y')]
 
 
+def parallel_horizontal_plates_resistive_wall_kicks(slicer, pipe_radius,
+                                                    length, conductivity,
+                                                    dt_min, n_turns_wake=1):
+    """ParallelHorizontalPlatesResistiveWall (wakes.py:643-656): Yokoya
+    X1 = pi^2/24, Y1 = pi^2/12, X2 = -pi^2/24, Y2 = pi^2/24, kicks in the
+    order of ResistiveWall.get_wake_kicks (wakes.py:577-609): dipole x,
+    quadrupole x, dipole y, quadrupole y."""
+    def wf(yokoya):
+        return resistive_wall_transverse(pipe_radius, length, conductivity,
+                                         dt_min, yokoya)
+    return [WakeKick(wf(np.pi**2 / 24.), slicer, n_turns_wake, 'xp', 'x'),
+            WakeKick(wf(-np.pi**2 / 24.), slicer, n_turns_wake, 'xp', None,
+                     quad='x'),
+            WakeKick(wf(np.pi**2 / 12.), slicer, n_turns_wake, 'yp', 'y'),
+            WakeKick(wf(np.pi**2 / 24.), slicer, n_turns_wake, 'yp', None,
+                     quad='y')]
+
+
 class WakeField(object):
     """WakeField.track, wakes.py:89-145."""
 
