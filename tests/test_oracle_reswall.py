@@ -6,8 +6,9 @@ machine's element order [RFSystems, TransverseSegmentMap, WakeField], the
 parallel horizontal plates resistive wall and UniformChargeSlicer(500,
 n_sigma_z=3) with the reference's random remainder draws (Python random,
 seed 7).  The oracle's vertical centroid over 1000 turns must equal the
-reference's to 1e-12 of its largest value (measured 2e-17 absolute: the
-centroid's summation order), and the growth rate fitted as the reference
+reference's to 1e-9 of its largest value (measured 2e-17 absolute on the
+x86 host that made the fixture, the centroid's summation order; the bar
+leaves room for another platform's libm over 1000 unstable turns), and the growth rate fitted as the reference
 test fits it must meet its bar (70e-4 per turn within 5 %; the fixture's
 bunch gives 7.23e-3)."""
 import os
@@ -64,7 +65,7 @@ def test_oracle_reproduces_reference_resistive_wall_growth():
         y[i] = beam.mean_y()
     ref = g['mean_y']
     scale = np.max(np.abs(ref))
-    assert np.max(np.abs(y - ref)) <= 1e-12 * scale, np.max(np.abs(y - ref))
+    assert np.max(np.abs(y - ref)) <= 1e-9 * scale, np.max(np.abs(y - ref))
     ampl = np.abs(hilbert(y))
     rate = linregress(np.arange(G.N_TURNS)[100:], np.log(ampl[100:]))[0]
     assert abs(rate - float(g['growth_rate'])) <= 1e-6 * abs(rate)
