@@ -9,8 +9,10 @@ namespace phk {
 
 size_t track_smem_bytes(int32_t dtype, int32_t Sa, int32_t Sp) {
     int nh, ks, st;
+    // a turn's pending kicks: four dipolar kicks (resonator and resistive
+    // wall, both planes), staged as one summed table per plane in FP32
     return dtype == PHK_F64 ? smem_for<double>(Sa, Sp, 4, false, &nh, &ks, &st)
-                            : smem_for<float>(Sa, Sp, 4, true, &nh, &ks, &st);
+                            : smem_for<float>(Sa, Sp, 2, true, &nh, &ks, &st);
 }
 
 // Compile-time shape of a program (see TrackShape), from its op kinds.

@@ -443,10 +443,7 @@ static int launch_stats_t(const phk_coords* c, const phk_kick_set* pk,
     t.n = c->n;
     t.has_pk = pk != nullptr;
     t.load_mask = load_mask;
-    t.kicks_smem = pk ? (size_t)pk->n_kicks * pk->slicer.n_slices * sizeof(T) <=
-                            48 * 1024
-                      : 0;
-    plan_kick_comb<T>(pk, &t);
+    plan_kick_tables<T>(pk, &t);
     a.o = stats_out(c, s);
     a.mask = mask;
     for (int q = 0; q < 6; ++q)

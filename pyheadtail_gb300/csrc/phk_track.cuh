@@ -711,16 +711,19 @@ __device__ __forceinline__ void run_program_shape(const phk_program& prog,
 }
 
 // ===================================================================
-// per-slice accumulation in shared memory, deterministic
-//   Each warp owns a private histogram (count, sum x, sum y per slice).
-//   Lanes of a warp holding the same slice are found with match.any; they
-//   update the bin one after the other in lane order (rank steps separated
-//   by __syncwarp), so no atomics are needed and the sums do not depend on
-//   scheduling.  FP64 form: plain double sums.  FP32 form: Kahan (1965)
-//   compensated float sums, one (sum, compensation) float2 per bin.
-//   When the per-warp copies do not fit, warps share one histogram and the
-//   updates fall back to atomics (FP64 form only needs that above ~500
-//   slices; the FP32 form always fits up to PHK_MAX_SLICES / 8 warps).
+// per-slice accumulation in shared memory
+//
+// FP64 form and the batched kernels: each warp owns a private histogram
+//   (count, sum x, sum y per slice); lanes of a warp holding the same slice
+//   are serialised by bids (warp_accumulate), so a bin is updated in a fixed
+//   lane order and the sums do not depend on scheduling.  FP64: plain
+//   double sums; FP32 (batched kernel): Kahan (1965) compensated float sums,
+//   one (sum, compensation) float2 per bin.  When the per-warp copies do not
+//   fit the shared-memory plan, warps share copies through atomics.
+//
+// FP32 single-bunch kernel: exact fixed-point sums (FixHist below), one
+//   histogram per CTA updated with 32-bit integer atomics: integer addition
+//   is associative, so the sums are bit-identical whatever the order.
 // ===================================================================
 
 template <typename T>
@@ -807,6 +810,106 @@ __device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
     }
 }
 
+// -------------------------------------------------------------------
+// FixHist: exact, order-independent per-slice sums of FP32 coordinates.
+//
+// Every thread-block cluster agrees on one power-of-two scale per
+// coordinate, 2^k with k chosen from the largest finite |u| of the
+// cluster's first tiles so that it maps to [2^26, 2^27).  A value u becomes
+// the integer v = rint(u 2^k) (u 2^k is exact; the rounding is the only
+// approximation, at most 2^-28 of that largest value, below the FP32
+// rounding of u itself).  Level A, |u 2^k| < 2^30: v is split into three
+// digits d0 = v & 0x7ff, d1 = (v >> 11) & 0x3ff, d2 = v >> 21 (arithmetic)
+// that are added to 32-bit counters with shared-memory atomics; each digit
+// is below 2^11 in magnitude, so 2^20 values per counter cannot overflow
+// (a CTA adds its counters to level B every 2^20 values).  Level B, larger
+// finite values (2^30 <= |u 2^k| < 2^40, rare): 64-bit atomics at the same
+// scale on the cluster's partial column in global memory, zeroed by the
+// cluster's rank 0 before the first add.  Level C: NaN, +-inf and
+// |u 2^k| >= 2^40 set flag bits of the slice; the slice's sum then becomes
+// NaN (NaN, both infinities, or out of range) or +-inf, as a floating-point
+// sum would.  At the end rank 0 adds the digits of its cluster's CTAs and
+// the level-B sums as 64-bit integers, converts once to FP64 (x 2^-k) and
+// writes the partial column.  Every step is integer arithmetic or a fixed
+// sequence of FP64 operations: the result is bit-identical on every launch.
+// -------------------------------------------------------------------
+constexpr float kFixLevelA = 1073741824.0f;        // 2^30
+constexpr float kFixLevelB = 1099511627776.0f;     // 2^40
+constexpr int64_t kFixMaxPerCta = (int64_t)1 << 20;  // values per counter
+
+// Levels B and C of one value (rare; kept out of line): v = u 2^k.
+static __device__ __noinline__ void fix_add_slow(long long* spill,
+                                                 unsigned* flag, int shift,
+                                                 float u, float v) {
+    if (fabsf(v) < kFixLevelB) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(spill),
+                  (unsigned long long)__float2ll_rn(v));
+        return;
+    }
+    // 1 NaN, 2 +inf, 4 -inf, 8 finite beyond the 64-bit range
+    const unsigned b = isnan(u) ? 1u : (isinf(u) ? (u > 0.f ? 2u : 4u) : 8u);
+    atomicOr(flag, b << shift);
+}
+
+// level-B columns of a CTA's FixHist (read on the rare slow path only):
+// element s of coordinate q at spill[q] + s * stride
+struct FixSpill {
+    long long* spill[2];
+    int64_t stride;
+};
+
+struct FixHist {
+    int* cnt;             // [S] counts
+    int* dig;             // [6][S]: x d0 d1 d2, y d0 d1 d2
+    unsigned* flag;       // [(S + 3) / 4]: one byte per slice, x low nibble
+    const FixSpill* sp;   // in shared memory
+    int S;
+    float scale[2];       // 2^k of x and y
+
+    __device__ __forceinline__ void add_q(int q, int s, float u) const {
+        const float v = u * scale[q];
+        if (fabsf(v) < kFixLevelA) {
+            const int iv = __float2int_rn(v);
+            int* d = dig + 3 * q * S + s;
+            atomicAdd(d, iv & 0x7ff);
+            atomicAdd(d + S, (iv >> 11) & 0x3ff);
+            atomicAdd(d + 2 * S, iv >> 21);
+        } else {
+            fix_add_slow(sp->spill[q] + (int64_t)s * sp->stride,
+                         flag + (s >> 2), 8 * (s & 3) + 4 * q, u, v);
+        }
+    }
+    __device__ __forceinline__ void add(int s, float x, float y) const {
+        atomicAdd(cnt + s, 1);
+        add_q(0, s, x);
+        add_q(1, s, y);
+    }
+};
+
+// 2^k, the FixHist scale for the largest finite magnitude m (as float bits;
+// 0 when there is none): m 2^k in [2^26, 2^27)
+__device__ __forceinline__ float fix_scale(unsigned mbits) {
+    int k = 40;                         // no finite non-zero value seen
+    if (mbits != 0u && mbits < 0x7f800000u) {
+        const int e = (int)(mbits >> 23) - 127;   // denormals: e = -127
+        k = 26 - e;
+    }
+    k = k > 100 ? 100 : (k < -100 ? -100 : k);
+    return ldexpf(1.0f, k);
+}
+
+// the FP64 value of a slice sum from its 64-bit total and flag nibble
+__device__ __forceinline__ double fix_value(long long total, unsigned fl,
+                                            float scale) {
+    if (fl) {
+        if ((fl & 9u) || (fl & 6u) == 6u)
+            return __longlong_as_double(0x7ff8000000000000ll);
+        return (fl & 2u) ? __longlong_as_double(0x7ff0000000000000ll)
+                         : __longlong_as_double((long long)0xfff0000000000000ull);
+    }
+    return (double)total * (1.0 / (double)scale);
+}
+
 // ===================================================================
 // the fused track kernel
 // ===================================================================
@@ -864,6 +967,8 @@ struct TrackArgs {
     int32_t kick_comb;   // kicks staged as one summed table per target
     int32_t comb_slot[3];  // table of target xp, yp, dp (-1: none)
     uint32_t wait_limit;   // polls of a copy wait before giving up
+    int32_t n_tables;      // kick tables staged (summed targets or kicks)
+    int32_t reserved;
 };
 
 template <typename T>
@@ -880,26 +985,34 @@ template <>
 __device__ __forceinline__ float tmul<float>(float a, float b) { return a * b; }
 
 // shared memory layout, in this order (every region 16-byte aligned):
-//   histogram words  [3][n_hist][Sa]   (sum x, sum y as Hist<T>::Word; count
-//                                       as int in the third region)
+//   histogram: bid-serialised words [3][n_hist][Sa] (sum x, sum y as
+//              Hist<T>::Word; count as int in the third region), or with
+//              `fix` (FP32 single bunch) the FixHist counters: count [Sa],
+//              digits [6][Sa], flag bytes [Sa] (ints)
 //   accumulation edges [Sa + 1] T, pending-kick edges [Sp + 1] T,
-//   kick tables [n_kicks][Sp] T (when staged), bid tags [n_hist][Sa] int,
-//   TMA ring [stages][6][tile] T, one mbarrier per stage
+//   kick tables [n_tables][Sp] T (when staged), bid tags [n_hist][Sa] int
+//   (none with `fix`), TMA ring [stages][6][tile] T, one mbarrier per stage
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
 
 template <typename T>
 __host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
-                                                    int n_kicks, int kicks_smem,
+                                                    int n_tables, int kicks_smem,
                                                     int stages, int tile,
-                                                    size_t* off) {
+                                                    size_t* off, bool fix = false) {
     size_t b = 0;
-    off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x words
-    off[1] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum y words
-    off[2] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // count
+    if (fix) {
+        off[0] = b; b = align16(b + (size_t)4 * Sa);              // count
+        off[1] = b; b = align16(b + (size_t)4 * 6 * Sa);          // digits
+        off[2] = b; b = align16(b + (size_t)4 * ((Sa + 3) / 4));  // flags
+    } else {
+        off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x words
+        off[1] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum y words
+        off[2] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // count
+    }
     off[3] = b; b = align16(b + sizeof(T) * (Sa > 0 ? Sa + 1 : 0));
     off[4] = b; b = align16(b + sizeof(T) * (Sp > 0 ? Sp + 1 : 0));
-    off[5] = b; b = align16(b + (kicks_smem ? sizeof(T) * (size_t)n_kicks * Sp : 0));
-    off[6] = b; b = align16(b + (size_t)4 * n_hist * Sa);   // bid tags
+    off[5] = b; b = align16(b + (kicks_smem ? sizeof(T) * (size_t)n_tables * Sp : 0));
+    off[6] = b; b = align16(b + (fix ? 0 : (size_t)4 * n_hist * Sa));  // bid tags
     off[7] = b; b = align16(b + (size_t)stages * 6 * tile * sizeof(T));
     off[8] = b; b = align16(b + (size_t)8 * stages);         // mbarriers
     return b;
@@ -926,7 +1039,7 @@ template <>
 struct Bins<float> {
     const float* e;
     int S, neg;
-    float tail, iw, e0, eS, mg;
+    float tail, iw, mg;   // tail = e[0]
     // mg bounds |u - u_ref|, u = (zz - e0) * iw the FP32 position in slice
     // units and u_ref the reference's (z - tail) / width of the same z.
     // The table's end edges lie within one FP32 ulp of the real cuts, so
@@ -937,7 +1050,7 @@ struct Bins<float> {
     // path off.
     __device__ __forceinline__ void init(const float* edges, int n, int negate) {
         e = edges; S = n; neg = negate;
-        e0 = e[0]; eS = e[S];
+        const float e0 = e[0], eS = e[S];
         tail = e0;
         const float span = eS - e0;
         iw = span > 0.f ? (float)S / span : 0.f;
@@ -986,7 +1099,7 @@ struct Bins<float> {
 #pragma unroll
         for (int j = 0; j < VEC; ++j) {
             if (out[j] != -2) continue;
-            if (!(zz[j] >= e0) || !(zz[j] < eS)) { out[j] = -1; continue; }
+            if (!(zz[j] >= tail) || !(zz[j] < e[S])) { out[j] = -1; continue; }
             int kk = (int)((zz[j] - tail) * iw);
             kk = kk < 0 ? 0 : (kk > S - 1 ? S - 1 : kk);
             float l = e[kk], h = e[kk + 1];
@@ -1159,13 +1272,14 @@ struct TrackCtx {
     int* tag;
     unsigned epoch;
     bool shared_hist;
+    FixHist fix;          // FP32 single-bunch accumulation
 };
 
 // One tile of VEC particles per thread, already in registers: pending
 // kicks, element program, slice accumulation; then the stores.  All threads
 // of the CTA call this together (the accumulation is warp-synchronous);
 // lanes whose particles are past the end pass live = false.
-template <typename T, int VEC, int SHAPE, bool FULL>
+template <typename T, int VEC, int SHAPE, bool FULL, bool FIX = false>
 __device__ __forceinline__ void run_tile(const phk_program& prog,
                                          const phk_kick_set& pk,
                                          const phk_accum& acc,
@@ -1189,8 +1303,12 @@ __device__ __forceinline__ void run_tile(const phk_program& prog,
                     s >= 0 ? s
                            : outside_index((double)t.c[PHK_Z][j],
                                            acc.slicer.tail, acc.slicer.width);
-            warp_accumulate<T>(s, t.c[PHK_X][j], t.c[PHK_Y][j], cx.hx, cx.hy,
-                               cx.hc, cx.tag, cx.epoch, cx.shared_hist);
+            if constexpr (FIX) {
+                if (s >= 0) cx.fix.add(s, (float)t.c[PHK_X][j], (float)t.c[PHK_Y][j]);
+            } else {
+                warp_accumulate<T>(s, t.c[PHK_X][j], t.c[PHK_Y][j], cx.hx, cx.hy,
+                                   cx.hc, cx.tag, cx.epoch, cx.shared_hist);
+            }
         }
     }
     // 4. stores of the coordinates the tile changed
@@ -1238,6 +1356,32 @@ constexpr size_t kF64SmemBudget = 112 * 1024;
 
 // polls of one mbarrier phase before a kernel gives up (order of a second)
 constexpr unsigned kWaitLimit = 1u << 22;
+// stages of the TMA ring at most
+constexpr int kMaxStages = 4;
+
+// FixHist counters are added to the level-B column after this many tiles
+// of a CTA (kFixMaxPerCta values per counter at most)
+template <int TILE>
+constexpr int64_t fix_flush_tiles() { return kFixMaxPerCta / TILE; }
+
+// Adds the FixHist digits of this CTA to the level-B column and clears them
+// (all threads, between two barriers).
+__device__ __forceinline__ void fix_flush(const FixHist& f, int tid,
+                                          int nthreads) {
+    for (int s = tid; s < f.S; s += nthreads) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            int* d = f.dig + 3 * q * f.S + s;
+            const long long t = (long long)d[0] + ((long long)d[f.S] << 11) +
+                                ((long long)d[2 * f.S] << 21);
+            if (t != 0)
+                atomicAdd(reinterpret_cast<unsigned long long*>(
+                              f.sp->spill[q] + (int64_t)s * f.sp->stride),
+                          (unsigned long long)t);
+            d[0] = 0; d[f.S] = 0; d[2 * f.S] = 0;
+        }
+    }
+}
 
 // FP32 launches aim at four resident CTAs per SM (<= 64 registers), FP64
 // ones at two (<= 128 registers; the FP64 pipe needs the warps to hide
@@ -1248,37 +1392,54 @@ track_kernel(const __grid_constant__ phk_program prog,
              const __grid_constant__ phk_kick_set pk,
              const __grid_constant__ phk_accum acc, const TrackArgs a) {
     using W = typename Hist<T>::Word;
+    // FP32: exact fixed-point slice sums (FixHist); FP64: bid-serialised
+    // per-warp histograms
+    constexpr bool FIX = std::is_same<T, float>::value;
+    namespace cg = cooperative_groups;
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int TILE = kTrackThreads * VEC;
     const int Sa = a.has_acc ? acc.slicer.n_slices : 0;
     const int Sp = a.has_pk ? pk.slicer.n_slices : 0;
-    const int nk = a.has_pk ? pk.n_kicks : 0;
     size_t off[9];
-    track_smem_layout<T>(Sa, Sp, a.n_hist, nk, a.kicks_smem, a.stages, TILE,
-                         off);
+    track_smem_layout<T>(Sa, Sp, a.n_hist, a.n_tables, a.kicks_smem, a.stages,
+                         TILE, off, FIX);
     W* hsx = reinterpret_cast<W*>(smem + off[0]);
     W* hsy = reinterpret_cast<W*>(smem + off[1]);
-    int* hcnt = reinterpret_cast<int*>(smem + off[2]);
+    int* hcnt = reinterpret_cast<int*>(smem + (FIX ? off[0] : off[2]));
+    int* fdig = reinterpret_cast<int*>(smem + off[1]);
+    unsigned* fflag = reinterpret_cast<unsigned*>(smem + off[2]);
     T* eacc = reinterpret_cast<T*>(smem + off[3]);
     T* epk = reinterpret_cast<T*>(smem + off[4]);
     T* ktab = reinterpret_cast<T*>(smem + off[5]);
     int* htag = reinterpret_cast<int*>(smem + off[6]);
     T* ring = reinterpret_cast<T*>(smem + off[7]);
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + off[8]);
-    __shared__ int s_fail;
+    __shared__ unsigned s_max[2];   // FixHist: largest finite |x|, |y| bits
+    __shared__ FixSpill s_spill;
+    // TMA ring: warps that finished each stage, the last tile issued into
+    // each stage (-1: none), a wait that gave up somewhere in the CTA
+    __shared__ int s_rel[kMaxStages], s_last[kMaxStages], s_abort;
 
     const int tid = threadIdx.x;
     if (tid == 0) {
-        s_fail = 0;
+        s_max[0] = s_max[1] = 0u;
+        s_abort = 0;
+        for (int st = 0; st < kMaxStages; ++st) s_rel[st] = 0, s_last[st] = -1;
         for (int st = 0; st < a.stages; ++st) mbar_init(bars + st, 1);
         if (a.stages > 0) mbar_fence_init();
     }
     if (a.has_acc) {
         const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
         for (int i = tid; i <= Sa; i += blockDim.x) stage_edge<T>(eacc, i, e[i]);
-        for (int i = tid; i < a.n_hist * Sa; i += blockDim.x) {
-            Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
-            hcnt[i] = 0; htag[i] = 0;
+        if constexpr (FIX) {
+            for (int i = tid; i < Sa; i += blockDim.x) hcnt[i] = 0;
+            for (int i = tid; i < 6 * Sa; i += blockDim.x) fdig[i] = 0;
+            for (int i = tid; i < (Sa + 3) / 4; i += blockDim.x) fflag[i] = 0u;
+        } else {
+            for (int i = tid; i < a.n_hist * Sa; i += blockDim.x) {
+                Hist<T>::zero(hsx + i); Hist<T>::zero(hsy + i);
+                hcnt[i] = 0; htag[i] = 0;
+            }
         }
     }
     if (a.has_pk) stage_pending<T>(pk, a, epk, ktab, tid, blockDim.x);
@@ -1300,70 +1461,193 @@ track_kernel(const __grid_constant__ phk_program prog,
     cx.epoch = 0;
     cx.shared_hist = a.n_hist < (int)(blockDim.x >> 5);
 
-    if (a.stages > 0) {
-        // ---- full tiles through a TMA ring: thread 0 keeps `stages` tiles
-        // of bulk copies in flight while the CTA computes
-        const int64_t full_tiles = a.n / TILE;
-        const int64_t mine = blockIdx.x < full_tiles
-                                 ? (full_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x
-                                 : 0;
-        int nq = 0;
-        for (int q = 0; q < 6; ++q) nq += (a.load_mask >> q) & 1;
-        const unsigned stage_bytes = (unsigned)(nq * TILE * sizeof(T));
-        auto issue = [&](int64_t k) {
-            const int st = (int)(k % a.stages);
-            const int64_t tile = blockIdx.x + k * gridDim.x;
-            fence_proxy_async_smem();
-            mbar_expect_tx(bars + st, stage_bytes);
-            for (int q = 0; q < 6; ++q)
-                if ((a.load_mask >> q) & 1)
-                    bulk_g2s(ring + ((size_t)st * 6 + q) * TILE,
-                             cx.cp[q] + tile * TILE, TILE * sizeof(T),
-                             bars + st);
-        };
-        int64_t issued = 0;
-        if (tid == 0)
-            for (; issued < mine && issued < a.stages; ++issued) issue(issued);
-        int64_t k = 0;
-        for (; k < mine; ++k) {
-            const int st = (int)(k % a.stages);
-            const unsigned parity = (unsigned)((k / a.stages) & 1);
-            if (!mbar_wait(bars + st, parity, a.wait_limit)) s_fail = 1;
-            __syncthreads();
-            if (s_fail) break;
-            Tile<T, VEC> t;
-            const T* src = ring + (size_t)st * 6 * TILE + tid * VEC;
+    // partial column of this CTA's cluster
+    const bool clustered = a.has_acc && a.cluster > 1;
+    const unsigned crank = clustered ? cg::this_cluster().block_rank() : 0u;
+    const int column = clustered ? (int)(blockIdx.x / a.cluster) : (int)blockIdx.x;
+    const int G = acc.grid;
+    double* P = acc.partials;
+
+    const int64_t full_tiles = a.n / TILE;
+    const int64_t mine = (a.stages > 0 && blockIdx.x < full_tiles)
+                             ? (full_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x
+                             : 0;
+    const bool has_partial = a.stages > 0 && a.n % TILE != 0 &&
+                             blockIdx.x == (int)(full_tiles % gridDim.x);
+    int nq = 0;
+    for (int q = 0; q < 6; ++q) nq += (a.load_mask >> q) & 1;
+    const unsigned stage_bytes = (unsigned)(nq * TILE * sizeof(T));
+    // bulk copies of this CTA's k-th tile into stage st (one thread)
+    auto issue = [&](int64_t k, int st) {
+        const int64_t tile = blockIdx.x + k * gridDim.x;
+        fence_proxy_async_smem();
+        mbar_expect_tx(bars + st, stage_bytes);
+        for (int q = 0; q < 6; ++q)
+            if ((a.load_mask >> q) & 1)
+                bulk_g2s(ring + ((size_t)st * 6 + q) * TILE,
+                         cx.cp[q] + tile * TILE, TILE * sizeof(T), bars + st);
+        s_last[st] = (int)k;
+    };
+    if (a.stages > 0 && tid == 0)
+        for (int64_t k = 0; k < mine && k < a.stages; ++k) issue(k, (int)k);
+    bool bad = false;   // a bounded copy wait of this thread gave up
+
+    if constexpr (FIX) {
+        if (a.has_acc) {
+            // ---- the cluster's scale: largest finite |x|, |y| of the inputs
+            // of every member's first tile (the maps change them by factors
+            // of order one; larger values take level B)
+            unsigned m[2] = {0u, 0u};
+            auto see = [&](float u, int q) {
+                const unsigned b = __float_as_uint(u) & 0x7fffffffu;
+                if (b < 0x7f800000u && b > m[q]) m[q] = b;
+            };
+            if (mine > 0) {
+                bad = !mbar_wait(bars, 0u, a.wait_limit);
+                if (!bad) {
+                    const T* src = ring + tid * VEC;
 #pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                if ((a.load_mask >> q) & 1) {
-                    VecIO<T, VEC>::ld(src + (size_t)q * TILE, t.c[q]);
-                } else {
+                    for (int j = 0; j < VEC; ++j) {
+                        see(src[(size_t)PHK_X * TILE + j], 0);
+                        see(src[(size_t)PHK_Y * TILE + j], 1);
+                    }
+                }
+            } else {
+                const int64_t i0 = (a.stages > 0 ? full_tiles * TILE
+                                                 : (int64_t)blockIdx.x * TILE) +
+                                   tid * VEC;
+                if (a.stages == 0 || has_partial) {
 #pragma unroll
-                    for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
+                    for (int j = 0; j < VEC; ++j) {
+                        if (i0 + j < a.n) {
+                            see(cx.cp[PHK_X][i0 + j], 0);
+                            see(cx.cp[PHK_Y][i0 + j], 1);
+                        }
+                    }
                 }
             }
-            const int64_t i0 = (blockIdx.x + k * gridDim.x) * TILE + tid * VEC;
-            run_tile<T, VEC, SHAPE, true>(prog, pk, acc, a, cx, t, i0, true);
-            __syncthreads();                 // stage st fully read
-            if (tid == 0 && k + a.stages < mine) issue(k + a.stages), ++issued;
+            m[0] = __reduce_max_sync(0xffffffffu, m[0]);
+            m[1] = __reduce_max_sync(0xffffffffu, m[1]);
+            if ((tid & 31) == 0) {
+                atomicMax(&s_max[0], m[0]);
+                atomicMax(&s_max[1], m[1]);
+            }
+            if (tid == 0) {
+                s_spill.spill[0] = reinterpret_cast<long long*>(P) + (int64_t)Sa * G + column;
+                s_spill.spill[1] = reinterpret_cast<long long*>(P) + (int64_t)2 * Sa * G + column;
+                s_spill.stride = G;
+            }
+            // rank 0 clears its column's level-B sums before any member adds
+            if (crank == 0) {
+                for (int s = tid; s < Sa; s += blockDim.x) {
+                    reinterpret_cast<long long*>(P)[(int64_t)(Sa + s) * G + column] = 0;
+                    reinterpret_cast<long long*>(P)[(int64_t)(2 * Sa + s) * G + column] = 0;
+                }
+            }
+            unsigned M[2];
+            if (clustered) {
+                __threadfence();
+                cg::cluster_group cl = cg::this_cluster();
+                cl.sync();
+                M[0] = M[1] = 0u;
+                for (unsigned r = 0; r < cl.num_blocks(); ++r) {
+                    const unsigned* sm = cl.map_shared_rank(s_max, r);
+                    M[0] = max(M[0], sm[0]);
+                    M[1] = max(M[1], sm[1]);
+                }
+            } else {
+                __syncthreads();
+                M[0] = s_max[0];
+                M[1] = s_max[1];
+            }
+            cx.fix.cnt = hcnt;
+            cx.fix.dig = fdig;
+            cx.fix.flag = fflag;
+            cx.fix.sp = &s_spill;
+            cx.fix.S = Sa;
+            cx.fix.scale[0] = fix_scale(M[0]);
+            cx.fix.scale[1] = fix_scale(M[1]);
         }
-        if (s_fail) {
-            // report, then wait (bounded) for this CTA's copies in flight so
-            // that none lands in shared memory after the CTA has exited
+    }
+
+    if (a.stages > 0) {
+        // ---- full tiles through a TMA ring of `stages` stages.  Warps run
+        // decoupled: each waits for a stage's copies, processes its part of
+        // the tile and releases the stage; the warp whose release completes
+        // the stage issues the copies of the tile `stages` ahead into it.
+        // A wait that gives up marks the CTA aborted: no more copies are
+        // issued, the remaining tiles are skipped (every warp still takes
+        // part in the same barriers), and the copies in flight are drained.
+        const int nwarps = (int)(blockDim.x >> 5);
+        const int lane = tid & 31;
+        volatile int* abort_flag = &s_abort;
+        int st = 0;
+        unsigned ph = 0u;
+        for (int64_t k = 0; k < mine; ++k) {
+            bool ok = false;
+            if (!bad && !*abort_flag) {
+                ok = mbar_wait(bars + st, ph, a.wait_limit);
+                if (!ok) {
+                    bad = true;
+                    *abort_flag = 1;
+                }
+            }
+            if (ok) {
+                Tile<T, VEC> t;
+                const T* src = ring + (size_t)st * 6 * TILE + tid * VEC;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    if ((a.load_mask >> q) & 1) {
+                        VecIO<T, VEC>::ld(src + (size_t)q * TILE, t.c[q]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < VEC; ++j) t.c[q][j] = T(0);
+                    }
+                }
+                const int64_t i0 = (blockIdx.x + k * gridDim.x) * TILE + tid * VEC;
+                run_tile<T, VEC, SHAPE, true, FIX>(prog, pk, acc, a, cx, t, i0, true);
+            }
+            __syncwarp();                    // this warp's part of stage st read
+            if (lane == 0) {
+                __threadfence_block();
+                if (atomicAdd(&s_rel[st], 1) == nwarps - 1) {
+                    s_rel[st] = 0;
+                    if (k + a.stages < mine && !*abort_flag) issue(k + a.stages, st);
+                }
+            }
+            if (++st == a.stages) {
+                st = 0;
+                ph ^= 1u;
+            }
+            if constexpr (FIX) {
+                if (a.has_acc && (k + 1) % fix_flush_tiles<TILE>() == 0) {
+                    __syncthreads();
+                    fix_flush(cx.fix, tid, blockDim.x);
+                    __syncthreads();
+                }
+            }
+        }
+        __syncthreads();
+        if (s_abort) {
+            // report, then wait (bounded) for the last copies issued into
+            // each stage so that none lands in shared memory after the CTA
+            // has exited (earlier ones completed before their stage was
+            // released)
             if (tid == 0) {
                 if (prog.status) atomicMax(prog.status, PHK_DEV_TIMEOUT);
-                for (int64_t j = k; j < issued; ++j)
-                    mbar_wait(bars + (int)(j % a.stages),
-                              (unsigned)((j / a.stages) & 1), kWaitLimit);
+                for (int q = 0; q < a.stages; ++q)
+                    if (s_last[q] >= 0)
+                        mbar_wait(bars + q, (unsigned)((s_last[q] / a.stages) & 1),
+                                  kWaitLimit);
             }
             __syncthreads();
-        } else if (a.n % TILE != 0 && blockIdx.x == (int)(full_tiles % gridDim.x)) {
+        } else if (has_partial) {
             // ---- the partial last tile, plain loads
             const int64_t i0 = full_tiles * TILE + tid * VEC;
             const bool full = i0 + VEC <= a.n;
             Tile<T, VEC> t;
             load_tile_plain<T, VEC>(a, cx, t, i0, full);
-            run_tile<T, VEC, SHAPE, false>(prog, pk, acc, a, cx, t, i0, full);
+            run_tile<T, VEC, SHAPE, false, FIX>(prog, pk, acc, a, cx, t, i0, full);
         }
     } else {
         // ---- plain loads; every warp runs whole tiles (lanes past the end
@@ -1375,14 +1659,68 @@ track_kernel(const __grid_constant__ phk_program prog,
             const bool full = i0 + VEC <= a.n;
             Tile<T, VEC> t;
             load_tile_plain<T, VEC>(a, cx, t, i0, full);
-            run_tile<T, VEC, SHAPE, false>(prog, pk, acc, a, cx, t, i0, full);
+            run_tile<T, VEC, SHAPE, false, FIX>(prog, pk, acc, a, cx, t, i0, full);
+            if constexpr (FIX) {
+                if (a.has_acc && (it + 1) % fix_flush_tiles<TILE>() == 0) {
+                    __syncthreads();
+                    fix_flush(cx.fix, tid, blockDim.x);
+                    __syncthreads();
+                }
+            }
         }
     }
 
-    if (a.has_acc) {
+    if (!a.has_acc) return;
+    if constexpr (FIX) {
+        // ---- rank 0 adds its cluster's counters and level-B sums as 64-bit
+        // integers and writes the partial column in FP64
+        unsigned nb = 1;
+        if (clustered) {
+            __threadfence();                 // level-B adds before the barrier
+            cg::cluster_group cl = cg::this_cluster();
+            cl.sync();
+            nb = cl.num_blocks();
+        } else {
+            __syncthreads();
+        }
+        if (crank == 0) {
+            const long long* lp = reinterpret_cast<const long long*>(P);
+            for (int s = tid; s < Sa; s += blockDim.x) {
+                long long c = 0, tq[2];
+                unsigned fl = 0;
+                tq[0] = __ldcg(lp + (int64_t)(Sa + s) * G + column);
+                tq[1] = __ldcg(lp + (int64_t)(2 * Sa + s) * G + column);
+                for (unsigned r = 0; r < nb; ++r) {
+                    const int* rc = hcnt;
+                    const int* rd = fdig;
+                    const unsigned* rf = fflag;
+                    if (clustered) {
+                        cg::cluster_group cl = cg::this_cluster();
+                        rc = cl.map_shared_rank(hcnt, r);
+                        rd = cl.map_shared_rank(fdig, r);
+                        rf = cl.map_shared_rank(fflag, r);
+                    }
+                    c += rc[s];
+                    fl |= (rf[s >> 2] >> (8 * (s & 3))) & 0xffu;
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const int* d = rd + 3 * q * Sa + s;
+                        tq[q] += (long long)d[0] + ((long long)d[Sa] << 11) +
+                                 ((long long)d[2 * Sa] << 21);
+                    }
+                }
+                P[(int64_t)s * G + column] = (double)c;
+                P[(int64_t)(Sa + s) * G + column] =
+                    fix_value(tq[0], fl & 15u, cx.fix.scale[0]);
+                P[(int64_t)(2 * Sa + s) * G + column] =
+                    fix_value(tq[1], fl >> 4, cx.fix.scale[1]);
+            }
+        }
+        if (clustered) cg::this_cluster().sync();  // members keep their counters until read
+        return;
+    } else {
         __syncthreads();
-        // fold the per-warp copies into copy 0, in the storage precision
-        // (fixed order; no FP64 arithmetic in the FP32 form)
+        // fold the per-warp copies into copy 0 (fixed order)
         for (int s = tid; s < Sa; s += blockDim.x) {
             int c = hcnt[s];
             for (int k = 1; k < a.n_hist; ++k) {
@@ -1392,15 +1730,12 @@ track_kernel(const __grid_constant__ phk_program prog,
             }
             hcnt[s] = c;
         }
-        int column = blockIdx.x;
-        if (a.cluster > 1) {
+        if (clustered) {
             // fold the CTAs of the thread-block cluster into its rank 0
             // through distributed shared memory
-            namespace cg = cooperative_groups;
             cg::cluster_group cl = cg::this_cluster();
             cl.sync();
-            const unsigned rank = cl.block_rank();
-            if (rank == 0) {
+            if (crank == 0) {
                 for (int s = tid; s < Sa; s += blockDim.x) {
                     int c = hcnt[s];
                     for (unsigned r = 1; r < cl.num_blocks(); ++r) {
@@ -1412,13 +1747,10 @@ track_kernel(const __grid_constant__ phk_program prog,
                 }
             }
             cl.sync();  // members keep their shared memory until read
-            if (rank != 0) return;
-            column = blockIdx.x / a.cluster;
+            if (crank != 0) return;
         } else {
             __syncthreads();
         }
-        const int G = acc.grid;
-        double* P = acc.partials;
         for (int s = tid; s < Sa; s += blockDim.x) {
             P[(int64_t)s * G + column] = (double)hcnt[s];
             P[(int64_t)(Sa + s) * G + column] = Hist<T>::value(hsx + s);
@@ -1431,28 +1763,32 @@ track_kernel(const __grid_constant__ phk_program prog,
 // launch configuration
 // ===================================================================
 
-// Shared-memory plan of a launch: histogram copies (one private copy per
-// warp when they fit, else fewer copies shared with atomics) and TMA ring
-// stages (FP32 aligned launches), chosen so that two CTAs fit on an SM
-// whenever possible.
+// Shared-memory plan of a launch: histogram copies (FP64: one private copy
+// per warp when they fit, else fewer copies shared with atomics; FP32: the
+// one FixHist of the CTA) and TMA ring stages (FP32 aligned launches),
+// chosen so that the occupancy the kernel is compiled for is reached
+// whenever possible.  n_tables: kick tables staged per CTA.
 template <typename T>
-static size_t smem_for(int Sa, int Sp, int nk, bool tma, int* n_hist,
+static size_t smem_for(int Sa, int Sp, int n_tables, bool tma, int* n_hist,
                        int* kicks_smem, int* stages) {
+    constexpr bool fix = sizeof(T) == 4;
     const int warps = kTrackThreads / 32;
     const int tile = kTrackThreads * (sizeof(T) == 8 ? 2 : kF32Vec);
     const size_t budget = sizeof(T) == 8 ? kF64SmemBudget : kF32SmemBudget;
-    *kicks_smem = (size_t)nk * Sp * sizeof(T) <= 48 * 1024;
+    *kicks_smem = n_tables > 0 && (size_t)n_tables * Sp * sizeof(T) <= 48 * 1024;
     const int hist_opts[4] = {warps, 4, 2, 1};
+    const int n_hist_opts = fix ? 1 : 4;
     // ring stages (0: plain loads, the fallback for large slice counts)
     const int stage_opts[3] = {3, 2, 0};
     size_t off[9];
     size_t smallest = 0;
-    for (int hi = 0; hi < 4; ++hi) {
+    for (int hi = 0; hi < n_hist_opts; ++hi) {
         for (int si = 0; si < (tma ? 3 : 1); ++si) {
-            const int nh = Sa > 0 ? hist_opts[hi] : 1;
+            const int nh = (Sa > 0 && !fix) ? hist_opts[hi] : 1;
             const int st = tma ? stage_opts[si] : 0;
-            const size_t b = track_smem_layout<T>(Sa, Sp, nh, nk, *kicks_smem,
-                                                  st, tile, off);
+            const size_t b = track_smem_layout<T>(Sa, Sp, nh, n_tables,
+                                                  *kicks_smem, st, tile, off,
+                                                  fix);
             if (b <= budget) {
                 *n_hist = nh;
                 *stages = st;
@@ -1470,23 +1806,37 @@ static size_t smem_for(int Sa, int Sp, int nk, bool tma, int* n_hist,
     return smallest;
 }
 
-// FP32 form: dipolar kicks of one target are summed once per slice when
-// staged (quadrupolar kicks keep the per-kick loop); sets a->kick_comb and
-// a->comb_slot (a->kicks_smem already decided)
+// Kick tables a launch stages: with FP32 coordinates and dipolar kicks
+// only, the kicks of one target are summed once per slice into one table
+// per target (quadrupolar kicks keep the per-kick loop).  Sets
+// a->kicks_smem, a->kick_comb, a->comb_slot and a->n_tables.
 template <typename T>
-static void plan_kick_comb(const phk_kick_set* pk, TrackArgs* a) {
+static void plan_kick_tables(const phk_kick_set* pk, TrackArgs* a) {
     a->kick_comb = 0;
     a->comb_slot[0] = a->comb_slot[1] = a->comb_slot[2] = -1;
-    if (sizeof(T) != 4 || !pk || !a->kicks_smem) return;
-    bool dip = true;
-    for (int k = 0; k < pk->n_kicks; ++k) dip = dip && pk->quad[k] < 0;
-    if (!dip) return;
-    a->kick_comb = 1;
-    int n = 0;
-    for (int k = 0; k < pk->n_kicks; ++k) {
-        const int tg = pk->target[k];
-        const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
-        if (a->comb_slot[q] < 0) a->comb_slot[q] = n++;
+    a->n_tables = 0;
+    a->kicks_smem = 0;
+    if (!pk) return;
+    const int nk = pk->n_kicks, Sp = pk->slicer.n_slices;
+    bool dip = sizeof(T) == 4;
+    for (int k = 0; k < nk; ++k) dip = dip && pk->quad[k] < 0;
+    int slot[3] = {-1, -1, -1}, n = 0;
+    if (dip) {
+        for (int k = 0; k < nk; ++k) {
+            const int tg = pk->target[k];
+            const int q = tg == PHK_XP ? 0 : (tg == PHK_YP ? 1 : 2);
+            if (slot[q] < 0) slot[q] = n++;
+        }
+    }
+    const int tables = dip ? n : nk;
+    a->kicks_smem = tables > 0 && (size_t)tables * Sp * sizeof(T) <= 48 * 1024;
+    if (dip && a->kicks_smem) {
+        a->kick_comb = 1;
+        for (int q = 0; q < 3; ++q) a->comb_slot[q] = slot[q];
+        a->n_tables = n;
+    } else {
+        a->kicks_smem = nk > 0 && (size_t)nk * Sp * sizeof(T) <= 48 * 1024;
+        a->n_tables = nk;
     }
 }
 
@@ -1583,13 +1933,15 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     static phk_accum zero_acc;
     const int Sa = acc ? acc->slicer.n_slices : 0;
     const int Sp = pk ? pk->slicer.n_slices : 0;
-    const int nk = pk ? pk->n_kicks : 0;
     // the TMA ring needs 16-byte aligned coordinates (VEC > 1 launches)
     // and pays off for the memory-bound FP32 form
     const bool tma = VEC > 1 && sizeof(T) == 4;
-    const size_t smem = smem_for<T>(Sa, Sp, nk, tma, &a.n_hist,
-                                    &a.kicks_smem, &a.stages);
-    plan_kick_comb<T>(pk, &a);
+    plan_kick_tables<T>(pk, &a);
+    int kicks_smem = 0;
+    const size_t smem = smem_for<T>(Sa, Sp, a.n_tables, tma, &a.n_hist,
+                                    &kicks_smem, &a.stages);
+    if (kicks_smem != a.kicks_smem)
+        return set_error(PHK_EPARAM, "phk_track: inconsistent kick-table plan");
     if (smem > track_dynamic_smem_limit<T, VEC, SHAPE>())
         return set_error(PHK_ESIZE, "phk_track: %zu bytes of shared memory "
                          "needed for %d + %d slices", smem, Sa, Sp);
