@@ -48,12 +48,13 @@ def test_single_rank_needs_no_process_group():
 
 def test_reference_arm_line_keeps_the_contract():
     """bench.py --impl reference on the host: one JSON line with the arm's
-    metric, a cpu_baseline describing the run and an e2e equal to it with
-    no host-device bytes; rank 1 of a 2-rank launch prints nothing."""
+    metric and config, a cpu_baseline describing the run and an e2e equal
+    to it with no host-device bytes; rank 1 of a 2-rank launch prints
+    nothing.  (The small linear-map workload keeps the test short.)"""
     import json
     import subprocess
     cmd = [sys.executable, os.path.join(ROOT, 'bench.py'), '--impl',
-           'reference', '--steps', '3', '--warmup', '3']
+           'reference', '--steps', '3', '--warmup', '3', '--workload', 'c1']
     out = subprocess.run(cmd, capture_output=True, text=True, timeout=600,
                          cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
@@ -63,6 +64,10 @@ def test_reference_arm_line_keeps_the_contract():
     assert d['impl'] == 'reference'
     assert d['unit'] == 'macroparticle-turns/s' and d['higher_is_better']
     assert d['value'] > 0 and d['steps'] == 3 and d['warmup'] == 3
+    # the same workload description as the GPU arm's line
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d['config'] == bench.bench_config(bench.WORKLOADS['c1'])
     cb = d['cpu_baseline']
     assert cb['value'] == d['value'] and cb['cores'] >= 1
     assert cb['kind'] in ('port', 'reference') and cb['sample']
