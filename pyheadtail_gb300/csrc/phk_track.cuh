@@ -44,20 +44,25 @@ __device__ __forceinline__ double chroma_poly(const double* c, int n, int z,
     return r;
 }
 
+// The detuned map below feeds sin / cos of a per-particle phase, which no
+// FP64 evaluation reproduces bit for bit anyway; its products and sums are
+// therefore fused (one rounding per multiply-add) to save FP64 operations
+// on GB300's narrow FP64 pipe.  Maps without per-particle transcendentals
+// keep the reference's separately rounded order.
 __device__ __forceinline__ double amp_action(double c1, double twoa, double b,
                                              double u, double up) {
     // 1/2 * ((1+a^2)/b * u**2 + 2*a * u*up + b * up**2)
-    double s = mul(c1, mul(u, u));
-    if (twoa != 0.0) s = add(s, mul(mul(twoa, u), up));
-    s = add(s, mul(b, mul(up, up)));
-    return mul(0.5, s);
+    double s = c1 * u * u;
+    if (twoa != 0.0) s = fma(twoa * u, up, s);
+    s = fma(b * up, up, s);
+    return 0.5 * s;
 }
 
 __device__ __forceinline__ double ij_term(double I, double J, bool hi,
                                           bool hj, double cc, double ss) {
-    if (hi && hj) return add(mul(I, cc), mul(J, ss));
-    if (hi) return mul(I, cc);
-    if (hj) return mul(J, ss);
+    if (hi && hj) return fma(I, cc, J * ss);
+    if (hi) return I * cc;
+    if (hj) return J * ss;
     return 0.0;
 }
 
@@ -116,8 +121,8 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
             for (int j = 0; j < VEC; ++j) {
                 const double Jx = amp_action(c1x, tax, bx, x[j], xp[j]);
                 const double Jy = amp_action(c1y, tay, by, y[j], yp[j]);
-                phx[j] = add(phx[j], div_by(add(mul(ax, Jx), mul(axy, Jy)), p0, ip0));
-                phy[j] = add(phy[j], div_by(add(mul(ay, Jy), mul(ayx, Jx)), p0, ip0));
+                phx[j] = add(phx[j], div_by(fma(ax, Jx, axy * Jy), p0, ip0));
+                phy[j] = add(phy[j], div_by(fma(ay, Jy, ayx * Jx), p0, ip0));
             }
         }
     }
@@ -149,10 +154,10 @@ __device__ __forceinline__ void op_transverse(const phk_op& op,
             x[j] = sub(x[j], mul(Dx0, dp[j]));
             y[j] = sub(y[j], mul(Dy0, dp[j]));
         }
-        const double nx = add(mul(M00, x[j]), mul(M01, xp[j]));
-        const double nxp = add(mul(M10, x[j]), mul(M11, xp[j]));
-        const double ny = add(mul(M22, y[j]), mul(M23, yp[j]));
-        const double nyp = add(mul(M32, y[j]), mul(M33, yp[j]));
+        const double nx = fma(M00, x[j], M01 * xp[j]);
+        const double nxp = fma(M10, x[j], M11 * xp[j]);
+        const double ny = fma(M22, y[j], M23 * yp[j]);
+        const double nyp = fma(M32, y[j], M33 * yp[j]);
         x[j] = nx; xp[j] = nxp; y[j] = ny; yp[j] = nyp;
         if (disp) {
             x[j] = add(x[j], mul(Dx1, dp[j]));
@@ -195,6 +200,59 @@ __device__ __forceinline__ void op_rfkick(const phk_op& op,
         double s = mul(A, sin(phi));
         if (f & PHK_FLAG_P_INC) s = sub(s, pinc);
         dp = div_by(add(mul(dp, p0o), s), p0n, ip0n);
+        if (f & PHK_FLAG_DISPERSION) {
+            t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+    }
+}
+
+// Drift and RF kick of an RFSystems element (Drift, Kick, Drift), plain
+// form.  The kick's per-particle sine makes the step inexact whatever the
+// evaluation order, so around it the arithmetic is regrouped to save FP64
+// operations (GB300 runs FP64 at a small fraction of the FP32 rate): the
+// drift is one multiply-add with eta0 * L, the phase one multiply-add with
+// h 2 pi / C, and the momentum update
+//   dp' = (dp p0_old + A sin(phi) - dp_inc) / p0_new
+// is dp (p0_old / p0_new) + (A / p0_new) sin(phi) - dp_inc / p0_new with
+// the ratios formed once per thread (the ratio is exactly 1 without
+// acceleration).  The separately rounded forms above remain for other
+// element sequences.
+template <int VEC>
+__device__ __forceinline__ void op_drift_rf(const phk_op& op,
+                                            Tile<double, VEC>& t) {
+    const double br = op.p[0], etaL = op.p[1] * op.p[2];
+    const bool shrink = op.flags & PHK_FLAG_SHRINK;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        const double z = t.c[PHK_Z][j];
+        const double zz = shrink ? mul(br, z) : z;
+        t.c[PHK_Z][j] = fma(-etaL, t.c[PHK_DP][j], zz);
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void op_rfkick_rf(const phk_op& op,
+                                             Tile<double, VEC>& t) {
+    const double* p = op.p;
+    const int f = op.flags;
+    const double hk = p[0] * p[1] * p[11];   // h 2 pi / C
+    double off = 0.0;
+    if (f & PHK_FLAG_PHI_OFFSET) off = add(off, p[3]);
+    if (f & PHK_FLAG_PHI_LOCK) off = add(off, p[4]);
+    const double Ar = p[5] * p[12];          // A / p0_new
+    const double ratio = p[6] == p[8] ? 1.0 : p[6] * p[12];
+    const double pinc = (f & PHK_FLAG_P_INC) ? p[7] * p[12] : 0.0;
+    const double Dx = p[9], Dy = p[10];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+        double& dp = t.c[PHK_DP][j];
+        if (f & PHK_FLAG_DISPERSION) {
+            t.c[PHK_X][j] = sub(t.c[PHK_X][j], mul(Dx, dp));
+            t.c[PHK_Y][j] = sub(t.c[PHK_Y][j], mul(Dy, dp));
+        }
+        const double s = sin(fma(hk, t.c[PHK_Z][j], off));
+        dp = fma(dp, ratio, fma(Ar, s, -pinc));
         if (f & PHK_FLAG_DISPERSION) {
             t.c[PHK_X][j] = add(t.c[PHK_X][j], mul(Dx, dp));
             t.c[PHK_Y][j] = add(t.c[PHK_Y][j], mul(Dy, dp));
@@ -699,9 +757,15 @@ __device__ __forceinline__ void run_program_shape(const phk_program& prog,
         op_transverse<VEC, true>(prog.op[0], prog, t);
     } else if constexpr (SHAPE == SHAPE_T_RF) {
         op_transverse<VEC, true>(prog.op[0], prog, t);
-        op_drift<VEC>(prog.op[1], t);
-        op_rfkick<VEC>(prog.op[2], t);
-        op_drift<VEC>(prog.op[3], t);
+        if constexpr (std::is_same<T, double>::value) {
+            op_drift_rf<VEC>(prog.op[1], t);
+            op_rfkick_rf<VEC>(prog.op[2], t);
+            op_drift_rf<VEC>(prog.op[3], t);
+        } else {
+            op_drift<VEC>(prog.op[1], t);
+            op_rfkick<VEC>(prog.op[2], t);
+            op_drift<VEC>(prog.op[3], t);
+        }
     } else if constexpr (SHAPE == SHAPE_T_LIN) {
         op_transverse<VEC, true>(prog.op[0], prog, t);
         op_linear_long<VEC>(prog.op[1], t);
@@ -1806,9 +1870,10 @@ static size_t smem_for(int Sa, int Sp, int n_tables, bool tma, int* n_hist,
     return smallest;
 }
 
-// Kick tables a launch stages: with FP32 coordinates and dipolar kicks
-// only, the kicks of one target are summed once per slice into one table
-// per target (quadrupolar kicks keep the per-kick loop).  Sets
+// Kick tables a launch stages: with dipolar kicks only, the kicks of one
+// target are summed once per slice into one table per target (one rounding
+// per slice instead of one per kick and particle; quadrupolar kicks keep
+// the per-kick loop).  Sets
 // a->kicks_smem, a->kick_comb, a->comb_slot and a->n_tables.
 template <typename T>
 static void plan_kick_tables(const phk_kick_set* pk, TrackArgs* a) {
@@ -1818,7 +1883,7 @@ static void plan_kick_tables(const phk_kick_set* pk, TrackArgs* a) {
     a->kicks_smem = 0;
     if (!pk) return;
     const int nk = pk->n_kicks, Sp = pk->slicer.n_slices;
-    bool dip = sizeof(T) == 4;
+    bool dip = true;
     for (int k = 0; k < nk; ++k) dip = dip && pk->quad[k] < 0;
     int slot[3] = {-1, -1, -1}, n = 0;
     if (dip) {
