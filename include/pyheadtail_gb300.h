@@ -276,12 +276,14 @@ typedef struct phk_wake_set {
  * tables are equal form one table group and share its K columns.
  * Set n_slices, n_groups, group_lags (rows of each group's table) and
  * n_kicks, then phk_wake_tc_plan() fills group_k0, k_total, m_tiles,
- * splits and the sizes of a_hi / a_lo (uint16 elements each) and partials
- * (float elements).  phk_wake_tc_expand() writes the bfloat16 operand
- * a_hi / a_lo from tables[g] (double[group_lags[g]][2 S - 1], the layout
- * of phk_wake_kick.table); repeat it whenever a table changes.  Per turn,
- * phk_wake_tc_run() reads the moment ring (as phk_wake_set) and writes out[k]
- * = factor[k] * convolution, in out_dtype. */
+ * splits and the sizes of a_hi / a_lo (uint16 elements each: every table
+ * row, sum of group_lags x (2 S - 1)) and partials (float elements).
+ * phk_wake_tc_expand() writes the bfloat16 high / low parts of tables[g]
+ * (double[group_lags[g]][2 S - 1], the layout of phk_wake_kick.table) to
+ * a_hi / a_lo; repeat it whenever a table changes.  Per turn,
+ * phk_wake_tc_run() reads the moment ring (as phk_wake_set), builds the
+ * Toeplitz operand tiles from a_hi / a_lo in shared memory and writes
+ * out[k] = factor[k] * convolution, in out_dtype. */
 typedef struct phk_wake_tc {
     int32_t n_slices;
     int32_t ring_len;

@@ -15,12 +15,14 @@
 // ~2^-16 relative); D_hi = A_hi B^T and D_lo = A_lo B^T hold all four
 // products hi*hi, hi*lo, lo*hi, lo*lo, summed in the epilogue.
 //
-// A depends only on the tables (fixed cuts and energy: constant over the
-// run), so it is expanded once into the canonical no-swizzle K-major layout
-// of the tensor-core operand, one 16 KB block per (128-row tile, 64-column
-// chunk), and streamed with bulk copies.  B is built per chunk in shared
-// memory from the FP64 moment ring.  The K range is split across CTAs; a
-// fixed-order FP64 reduction of the split partials applies the factors.
+// A is never stored: a 128 x 64 tile of it is a window of at most two
+// rows of a table (191 consecutive samples per lag), so each CTA builds its
+// A tiles in shared memory, in the canonical no-swizzle K-major layout of
+// the tensor-core operand, from a bfloat16 hi / lo copy of the tables
+// (written once per table change; C3: 200 KB, read from L2).  B is built
+// per chunk in shared memory from the FP64 moment ring.  The K range is
+// split across CTAs; a fixed-order FP64 reduction of the split partials
+// applies the factors.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -38,6 +40,14 @@ constexpr int kTcStages = 3;
 constexpr int kTcMaxChunks = 8;    // K chunks per CTA (B staged up front)
 constexpr int kTcThreads = 256;
 constexpr unsigned kTcTileBytes = kTcM * kTcK * 2;   // 16 KB per A part
+constexpr int kTcBuildRows = kTcThreads / 8;          // rows per build pass
+
+// K columns of one lag: the S source slices padded to a multiple of 8 (so
+// that no 8-column segment of a tile row spans two lags); the padding
+// columns of B are zero
+__host__ __device__ __forceinline__ int lag_cols(int S) { return (S + 7) & ~7; }
+// bfloat16 table rows (a_hi / a_lo): 8 zeros, the 2 S - 1 samples, 9 zeros
+__host__ __device__ __forceinline__ int row_stride(int S) { return 2 * S + 16; }
 constexpr unsigned kTcBBytes = kTcN * kTcK * 2;      // 2 KB
 constexpr unsigned kTcWaitLimit = 1u << 22;
 
@@ -137,40 +147,45 @@ __device__ __forceinline__ void split_bf16(double x, __nv_bfloat16* hi,
 }
 
 // K index -> (group, lag, source slice); false past the groups' columns
+// and on the padding columns of a lag
 __device__ __forceinline__ bool decode_k(const phk_wake_tc& w, int kg, int* g,
                                          int* a, int* j) {
+    const int SC = lag_cols(w.n_slices);
     int gg = w.n_groups - 1;
     while (gg > 0 && kg < w.group_k0[gg]) --gg;
     const int r = kg - w.group_k0[gg];
     if (r < 0) return false;
-    const int aa = r / w.n_slices;
+    const int aa = r / SC;
     if (aa >= w.group_lags[gg]) return false;
+    const int jj = r - aa * SC;
+    if (jj >= w.n_slices) return false;
     *g = gg;
     *a = aa;
-    *j = r - aa * w.n_slices;
+    *j = jj;
     return true;
 }
 
-// ------------------------------------------------------------ expansion
-__global__ void wake_expand_kernel(const __grid_constant__ phk_wake_tc w) {
-    const int S = w.n_slices;
-    const int n_chunks = w.k_total / kTcK;
-    const int64_t total = (int64_t)w.m_tiles * kTcM * w.k_total;
+// ------------------------------------------------------------ table split
+// bfloat16 hi / lo parts of every table row: sample t of lag a of group g
+// at row_stride(S) * R + 8 + t, R = group_k0[g] / lag_cols(S) + a (the
+// padding elements are zero)
+__global__ void wake_split_kernel(const __grid_constant__ phk_wake_tc w) {
+    const int S = w.n_slices, L = 2 * S - 1, Ls = row_stride(S);
+    const int SC = lag_cols(S);
+    const int rows = w.group_k0[w.n_groups - 1] / SC + w.group_lags[w.n_groups - 1];
+    const int64_t total = (int64_t)rows * Ls;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(e / w.k_total);
-        const int kg = (int)(e - (int64_t)i * w.k_total);
-        double v = 0.0;
-        int g, a, j;
-        if (i < S && decode_k(w, kg, &g, &a, &j))
-            v = w.tables[g][(int64_t)a * (2 * S - 1) + i - j + S - 1];
-        const int mt = i / kTcM, ch = kg / kTcK;
-        const int64_t at = ((int64_t)mt * n_chunks + ch) * (kTcM * kTcK) +
-                           tile_offset(i % kTcM, kg % kTcK);
+        const int row = (int)(e / Ls);
+        const int t = (int)(e - (int64_t)row * Ls) - 8;
+        int g = w.n_groups - 1;
+        while (g > 0 && row < w.group_k0[g] / SC) --g;
+        const int a = row - w.group_k0[g] / SC;
+        const double v = (t >= 0 && t < L) ? w.tables[g][(int64_t)a * L + t] : 0.0;
         __nv_bfloat16 h, l;
         split_bf16(v, &h, &l);
-        reinterpret_cast<__nv_bfloat16*>(w.a_hi)[at] = h;
-        reinterpret_cast<__nv_bfloat16*>(w.a_lo)[at] = l;
+        reinterpret_cast<__nv_bfloat16*>(w.a_hi)[e] = h;
+        reinterpret_cast<__nv_bfloat16*>(w.a_lo)[e] = l;
     }
 }
 
@@ -184,9 +199,8 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr unsigned kStage = 2 * kTcTileBytes;
     unsigned char* bsm = smem + kTcStages * kStage;
-    unsigned long long* full = reinterpret_cast<unsigned long long*>(
+    unsigned long long* done = reinterpret_cast<unsigned long long*>(
         bsm + kTcMaxChunks * kTcBBytes);
-    unsigned long long* done = full + kTcStages;
     unsigned long long* fin = done + kTcStages;
     unsigned* s_taddr = reinterpret_cast<unsigned*>(fin + 1);
     __shared__ int s_fail;
@@ -201,10 +215,7 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
 
     if (tid == 0) {
         s_fail = 0;
-        for (int s = 0; s < kTcStages; ++s) {
-            mbar_init(full + s, 1);
-            mbar_init(done + s, 1);
-        }
+        for (int s = 0; s < kTcStages; ++s) mbar_init(done + s, 1);
         mbar_init(fin, 1);
         mbar_fence_init();
     }
@@ -217,52 +228,100 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
     tc_fence_after_sync();
     const unsigned taddr = *s_taddr;
 
-    const __nv_bfloat16* ahi = reinterpret_cast<const __nv_bfloat16*>(w.a_hi);
-    const __nv_bfloat16* alo = reinterpret_cast<const __nv_bfloat16*>(w.a_lo);
-    auto issue = [&](int it) {
-        const int st = it % kTcStages;
-        const int64_t blk = ((int64_t)mt * n_chunks + c0 + it) * (kTcM * kTcK);
+    // A tile of chunk c0 + it into stage st.  An 8-column segment of a
+    // tile row lies within one lag (lag_cols), so its eight elements,
+    // sample i - j + S - 1 for j = j0 .. j0 + 7, are eight consecutive
+    // samples of one table row in descending order: five aligned 32-bit
+    // loads, four byte permutes, one 16-byte store in the canonical
+    // layout.  Thread t fills segment t & 7 of rows (t >> 3) + 32 m; rows
+    // past the slices and columns past the groups are zero.
+    const int SC = lag_cols(S), Ls = row_stride(S);
+    const int k_valid = w.group_k0[w.n_groups - 1] + w.group_lags[w.n_groups - 1] * SC;
+    const unsigned* thi = reinterpret_cast<const unsigned*>(w.a_hi);
+    const unsigned* tlo = reinterpret_cast<const unsigned*>(w.a_lo);
+    auto build = [&](int it, int st) {
+        const int c = tid & 7;
+        const int kg0 = (c0 + it) * kTcK + 8 * c;
+        const int R = kg0 / SC;
+        const int j0 = kg0 - R * SC;
+        const bool cols = kg0 < k_valid;
         unsigned char* dst = smem + st * kStage;
-        fence_proxy_async_smem();
-        mbar_expect_tx(full + st, 2 * kTcTileBytes);
-        bulk_g2s(dst, ahi + blk, kTcTileBytes, full + st);
-        bulk_g2s(dst + kTcTileBytes, alo + blk, kTcTileBytes, full + st);
-    };
-    int issued = 0;
-    if (tid == 0)
-        for (; issued < nc && issued < kTcStages; ++issued) issue(issued);
-
-    // B of every chunk of this CTA, while the first A copies are in flight
-    for (int e = tid; e < nc * kTcN * kTcK; e += kTcThreads) {
-        const int c = e / (kTcN * kTcK);
-        const int r = e - c * (kTcN * kTcK);
-        const int n = r / kTcK, kk = r - n * kTcK;
-        double v = 0.0;
-        int g, a, j;
-        if (n < 2 * nk && decode_k(w, (c0 + c) * kTcK + kk, &g, &a, &j)) {
-            const int k = n < nk ? n : n - nk;
-            if (w.group_of[k] == g && a < w.n_lags[k]) {
-                const int slot =
-                    ((w.head - a) % w.ring_len + w.ring_len) % w.ring_len;
-                v = w.moments[((int64_t)slot * 3 + w.source[k]) * S + j];
+        constexpr int kRows = kTcM / kTcBuildRows;
+        unsigned h[kRows][5], l[kRows][5];
+        // every load of the tile first (one round trip), then the permutes
+#pragma unroll
+        for (int m = 0; m < kRows; ++m) {
+            const int i = mt * kTcM + (tid >> 3) + kTcBuildRows * m;
+            // elements e_q = T[base + 7 - q], q = 0..7
+            const int64_t base = (int64_t)R * Ls + 8 + (S - 1 - j0 + i) - 7;
+            const int64_t w0 = base >> 1;          // 32-bit word index
+            const bool on = cols && i < S;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                h[m][q] = on ? __ldg(thi + w0 + q) : 0u;
+                l[m][q] = on ? __ldg(tlo + w0 + q) : 0u;
             }
         }
-        __nv_bfloat16 h, l;
-        split_bf16(v, &h, &l);
-        reinterpret_cast<__nv_bfloat16*>(bsm + c * kTcBBytes)[tile_offset(n, kk)] =
-            n < nk ? h : l;
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
+#pragma unroll
+        for (int m = 0; m < kRows; ++m) {
+            const int r = (tid >> 3) + kTcBuildRows * m;
+            const int i = mt * kTcM + r;
+            const unsigned sel = ((S - 1 - j0 + i) & 1) ? 0x5476u : 0x7610u;
+            const uint4 vh = make_uint4(
+                __byte_perm(h[m][4], h[m][3], sel), __byte_perm(h[m][3], h[m][2], sel),
+                __byte_perm(h[m][2], h[m][1], sel), __byte_perm(h[m][1], h[m][0], sel));
+            const uint4 vl = make_uint4(
+                __byte_perm(l[m][4], l[m][3], sel), __byte_perm(l[m][3], l[m][2], sel),
+                __byte_perm(l[m][2], l[m][1], sel), __byte_perm(l[m][1], l[m][0], sel));
+            const int off = tile_offset(r, 8 * c) * 2;
+            *reinterpret_cast<uint4*>(dst + off) = vh;
+            *reinterpret_cast<uint4*>(dst + kTcTileBytes + off) = vl;
+        }
+    };
 
-    // one thread issues the MMAs as the A stages land, refilling each stage
-    // once the MMAs that read it have completed
+    // B of every chunk of this CTA: one K column per thread and pass,
+    // decoded once, then the rows of its kicks (hi rows 0..nk-1, lo rows
+    // nk..2nk-1; the rest zero)
+    for (int e = tid; e < nc * kTcK; e += kTcThreads) {
+        const int c = e / kTcK, kk = e - c * kTcK;
+        int g = 0, a = 0, j = 0;
+        const bool on = decode_k(w, (c0 + c) * kTcK + kk, &g, &a, &j);
+        const int slot = ((w.head - a) % w.ring_len + w.ring_len) % w.ring_len;
+        __nv_bfloat16* col = reinterpret_cast<__nv_bfloat16*>(bsm + c * kTcBBytes);
+#pragma unroll
+        for (int k = 0; k < kTcN / 2; ++k) {
+            if (k >= nk) break;
+            double v = 0.0;
+            if (on && w.group_of[k] == g && a < w.n_lags[k])
+                v = w.moments[((int64_t)slot * 3 + w.source[k]) * S + j];
+            __nv_bfloat16 h, l;
+            split_bf16(v, &h, &l);
+            col[tile_offset(k, kk)] = h;
+            col[tile_offset(nk + k, kk)] = l;
+        }
+        for (int n = 2 * nk; n < kTcN; ++n)
+            col[tile_offset(n, kk)] = __float2bfloat16_rn(0.f);
+    }
+
+    // per chunk: the CTA builds its A tile in a free stage (the MMAs that
+    // read the stage before have completed), then one thread issues the
+    // MMAs asynchronously, so building the next tile overlaps them
     int it = 0;
-    if (tid == 0) {
-        for (; it < nc; ++it) {
-            const int st = it % kTcStages;
-            const unsigned par = (unsigned)((it / kTcStages) & 1);
-            if (!mbar_wait(full + st, par, wait_limit)) { s_fail = 1; break; }
+    for (; it < nc; ++it) {
+        const int st = it % kTcStages;
+        bool ok = true;
+        if (it >= kTcStages)
+            ok = mbar_wait(done + st, (unsigned)((it / kTcStages - 1) & 1),
+                           wait_limit);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) s_fail = 1;
+            break;
+        }
+        tc_fence_after_sync();
+        build(it, st);
+        fence_proxy_async_smem();      // generic writes -> tensor-core reads
+        __syncthreads();
+        if (tid == 0) {
             tc_fence_after_sync();
             const unsigned a_hi = smem_addr(smem + st * kStage);
             const unsigned a_lo = a_hi + kTcTileBytes;
@@ -277,26 +336,14 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
                           kTcIdesc, acc);
             }
             umma_commit(done + st);
-            if (issued < nc) {
-                if (!mbar_wait(done + st, par, wait_limit)) {
-                    s_fail = 1;
-                    ++it;
-                    break;
-                }
-                issue(issued++);
-            }
         }
     }
 
-    // completion of every MMA issued (commit arrives once all are done),
-    // then, after a failure, of the bulk copies still in flight (bounded)
+    // completion of every MMA issued (the commit arrives once all are
+    // done; bounded)
     if (tid == 0) {
         umma_commit(fin);
         if (!mbar_wait(fin, 0, kTcWaitLimit)) s_fail = 1;
-        if (s_fail)
-            for (int j = it; j < issued; ++j)
-                mbar_wait(full + j % kTcStages, (unsigned)((j / kTcStages) & 1),
-                          kTcWaitLimit);
     }
     tc_fence_before_sync();
     __syncthreads();
@@ -352,7 +399,7 @@ __global__ void wake_tc_reduce_kernel(const __grid_constant__ phk_wake_tc w) {
 
 size_t wake_tc_smem() {
     return kTcStages * 2 * kTcTileBytes + kTcMaxChunks * kTcBBytes +
-           (2 * kTcStages + 1) * 8 + 16;
+           (kTcStages + 1) * 8 + 16;
 }
 
 // K layout, tiles and split of a GEMM (fills k_total, m_tiles, splits and
@@ -361,7 +408,7 @@ int plan_wake_tc(phk_wake_tc* w, int64_t* a_elems, int64_t* partial_elems) {
     int64_t k = 0;
     for (int g = 0; g < w->n_groups; ++g) {
         w->group_k0[g] = (int32_t)k;
-        k += (int64_t)w->group_lags[g] * w->n_slices;
+        k += (int64_t)w->group_lags[g] * lag_cols(w->n_slices);
     }
     k = (k + kTcK - 1) / kTcK * kTcK;
     if (k > (int64_t)1 << 30)
@@ -377,18 +424,23 @@ int plan_wake_tc(phk_wake_tc* w, int64_t* a_elems, int64_t* partial_elems) {
     if (splits < need) splits = need;
     if (splits < 1) splits = 1;
     w->splits = splits;
-    if (a_elems) *a_elems = (int64_t)w->m_tiles * kTcM * k;
+    int64_t rows = 0;
+    for (int g = 0; g < w->n_groups; ++g) rows += w->group_lags[g];
+    if (a_elems) *a_elems = rows * row_stride(w->n_slices);
     if (partial_elems)
         *partial_elems = (int64_t)splits * w->n_kicks * w->m_tiles * kTcM;
     return PHK_OK;
 }
 
 int launch_wake_tc_expand(const phk_wake_tc* w, cudaStream_t st) {
-    const int64_t total = (int64_t)w->m_tiles * kTcM * w->k_total;
+    int64_t rows = 0;
+    for (int g = 0; g < w->n_groups; ++g) rows += w->group_lags[g];
+    const int64_t total = rows * row_stride(w->n_slices);
     int64_t blocks = (total + 255) / 256;
     const int64_t cap = (int64_t)device_info().sm_count * 8;
     if (blocks > cap) blocks = cap;
-    wake_expand_kernel<<<(unsigned)blocks, 256, 0, st>>>(*w);
+    if (blocks < 1) blocks = 1;
+    wake_split_kernel<<<(unsigned)blocks, 256, 0, st>>>(*w);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_wake_tc_expand launch: %s",

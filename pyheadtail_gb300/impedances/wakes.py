@@ -57,8 +57,9 @@ class _RingState(object):
 class _TensorWake(object):
     """Tensor-core convolution (phk_wake_tc_*) of the kicks of one WakeField
     in the FP32 form.  Kicks whose sampled tables are equal share a table
-    group; the bfloat16 operand is re-expanded whenever a table changes
-    (for fixed cuts and energy: during the first n_turns_wake turns)."""
+    group; the bfloat16 high / low parts of the tables are rewritten
+    whenever a table changes (for fixed cuts and energy: during the first
+    n_turns_wake turns); the GEMM builds its Toeplitz tiles from them."""
 
     def __init__(self, device):
         self.device = device

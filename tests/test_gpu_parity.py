@@ -86,7 +86,10 @@ def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9, emit_rtol=1e-7,
             np.testing.assert_array_equal(np.asarray(g), v,
                                           err_msg='%s %s' % (label, k))
         elif k.endswith(('_mean_x', '_mean_y')) and np.ndim(v) == 0:
-            assert abs(g - v) <= 1e-12 * max(abs(v), 1e-30) + 1e-18, (label, k)
+            tol = 1e-12 * max(abs(v), 1e-30) + 1e-18
+            if sens is not None and k in sens:
+                tol = max(tol, 4 * sens[k][0])
+            assert abs(g - v) <= tol, (label, k, g, v, tol)
         elif any(k.endswith('_' + c) for c in COORDS) and np.ndim(v) == 1 \
                 and len(k.split('_')) == 2:
             e = rms_err(g, v)
@@ -178,6 +181,11 @@ def _oracle_vs_gpu(spec, n_turns, record_turns=None, sensitivity=False):
             if (any(k.endswith('_' + c) for c in COORDS)
                 and np.ndim(ref[k]) == 1 and len(k.split('_')) == 2)
             or k.endswith(('_mean_x', '_mean_y')) and np.ndim(ref[k]) == 1}
+    for k in ref:
+        # bunch centroids: absolute change
+        if k.endswith(('_mean_x', '_mean_y')) and np.ndim(ref[k]) == 0:
+            d = abs(float(alt[k]) - float(ref[k]))
+            sens[k] = (d, d)
     return rec, ref, sens
 
 

@@ -80,8 +80,9 @@ def test_track_kernel_copy_wait_runs_out(lib):
 
 
 def test_tensor_core_wake_waits_run_out(lib):
-    """The GEMM's copy and MMA waits give up; the kernel drains, frees its
-    tensor memory, and the next call gives the FP64 convolution's kicks."""
+    """The GEMM's waits for the MMAs that read a shared-memory stage give
+    up; the kernel waits (bounded) for the MMAs in flight, frees its tensor
+    memory, and the next call gives the FP64 convolution's kicks."""
     import sys, os
     sys.path.insert(0, os.path.dirname(__file__))
     import test_gpu_wake_tc as T
