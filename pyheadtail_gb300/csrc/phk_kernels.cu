@@ -154,7 +154,11 @@ struct WakeArgs {
     phk_wake_set w;
 };
 
-// numpy path: one warp per (kick, target slice); lanes split the sources
+// numpy path: one warp per (kick, target slice); lanes split the sources.
+// Each lane keeps its partial sums over every stored turn and the warp
+// reduces once at the end (the reference sums each turn's convolution,
+// then the turns: the same terms, regrouped; GB300's FP64 pipe makes the
+// per-turn reductions the larger part of the cost otherwise).
 __device__ __forceinline__ void wake_conv_one(const phk_wake_set& w, int gw,
                                               int lane) {
     const int S = w.n_slices;
@@ -164,27 +168,27 @@ __device__ __forceinline__ void wake_conv_one(const phk_wake_set& w, int gw,
     const phk_wake_kick& kk = w.kick[k];
     if (kk.dense) return;
     const int L2 = 2 * S - 1;
-    double acc = 0.0;
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+    int slot = (w.head % w.ring_len + w.ring_len) % w.ring_len;
     for (int a = 0; a < kk.n_lags; ++a) {
-        const int slot = ((w.head - a) % w.ring_len + w.ring_len) % w.ring_len;
         const double* m = w.moments + ((int64_t)slot * 3 + kk.source) * S;
         const double* v = kk.table + (int64_t)a * L2 + i + S - 1;
-        double p0 = 0.0, p1 = 0.0;
         int j = lane;
-#pragma unroll 4
-        for (; j + 32 < S; j += 64) {
-            p0 = fma(m[j], v[-j], p0);
-            p1 = fma(m[j + 32], v[-j - 32], p1);
+        for (; j + 96 < S; j += 128) {
+            p0 = fma(__ldg(m + j), __ldg(v - j), p0);
+            p1 = fma(__ldg(m + j + 32), __ldg(v - j - 32), p1);
+            p2 = fma(__ldg(m + j + 64), __ldg(v - j - 64), p2);
+            p3 = fma(__ldg(m + j + 96), __ldg(v - j - 96), p3);
         }
-        if (j < S) p0 = fma(m[j], v[-j], p0);
-        double part = p0 + p1;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            part += __shfl_xor_sync(0xffffffffu, part, o);
-        acc = add(acc, part);
+        for (; j < S; j += 32) p0 = fma(__ldg(m + j), __ldg(v - j), p0);
+        slot = slot == 0 ? w.ring_len - 1 : slot - 1;
     }
+    double part = (p0 + p1) + (p2 + p3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        part += __shfl_xor_sync(0xffffffffu, part, o);
     if (lane == 0) {
-        const double r = mul(kk.factor, acc);
+        const double r = mul(kk.factor, part);
         if (w.out_dtype == PHK_F64)
             reinterpret_cast<double*>(kk.out)[i] = r;
         else
@@ -216,9 +220,51 @@ __device__ __forceinline__ void wake_dense_one(const phk_wake_set& w, int t) {
         reinterpret_cast<float*>(kk.out)[i] = (float)r;
 }
 
-__global__ void wake_conv_kernel(const __grid_constant__ phk_wake_set w) {
-    wake_conv_one(w, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
-                  threadIdx.x & 31);
+// Single-bunch numpy path: one CTA of kConvWarps warps per (kick, target
+// slice); warp w takes the stored turns w, w + kConvWarps, ...; the warps'
+// partial sums are added in a fixed order.  (One warp per output leaves
+// too few warps on GB300 to cover the load latency of a 50-turn history.)
+constexpr int kConvWarps = 8;
+__global__ void __launch_bounds__(kConvWarps * 32)
+wake_conv_kernel(const __grid_constant__ phk_wake_set w) {
+    __shared__ double part_w[kConvWarps];
+    const int S = w.n_slices;
+    const int k = blockIdx.x / S;
+    const int i = blockIdx.x - k * S;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (k >= w.n_kicks) return;
+    const phk_wake_kick& kk = w.kick[k];
+    if (kk.dense) return;
+    const int L2 = 2 * S - 1;
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+    for (int a = warp; a < kk.n_lags; a += kConvWarps) {
+        const int slot = ((w.head - a) % w.ring_len + w.ring_len) % w.ring_len;
+        const double* m = w.moments + ((int64_t)slot * 3 + kk.source) * S;
+        const double* v = kk.table + (int64_t)a * L2 + i + S - 1;
+        int j = lane;
+        for (; j + 96 < S; j += 128) {
+            p0 = fma(__ldg(m + j), __ldg(v - j), p0);
+            p1 = fma(__ldg(m + j + 32), __ldg(v - j - 32), p1);
+            p2 = fma(__ldg(m + j + 64), __ldg(v - j - 64), p2);
+            p3 = fma(__ldg(m + j + 96), __ldg(v - j - 96), p3);
+        }
+        for (; j < S; j += 32) p0 = fma(__ldg(m + j), __ldg(v - j), p0);
+    }
+    double part = (p0 + p1) + (p2 + p3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) part_w[warp] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = part_w[0];
+        for (int q = 1; q < kConvWarps; ++q) acc += part_w[q];
+        const double r = mul(kk.factor, acc);
+        if (w.out_dtype == PHK_F64)
+            reinterpret_cast<double*>(kk.out)[i] = r;
+        else
+            reinterpret_cast<float*>(kk.out)[i] = (float)r;
+    }
 }
 
 __global__ void wake_dense_kernel(const __grid_constant__ phk_wake_set w) {
@@ -231,12 +277,8 @@ int launch_wake(const phk_wake_set* w, cudaStream_t st) {
         if (w->kick[k].dense) any_dense = true; else any_conv = true;
     }
     const int S = w->n_slices;
-    if (any_conv) {
-        const int warps = w->n_kicks * S;
-        const int threads = 256;
-        wake_conv_kernel<<<(warps * 32 + threads - 1) / threads, threads, 0,
-                           st>>>(*w);
-    }
+    if (any_conv)
+        wake_conv_kernel<<<w->n_kicks * S, kConvWarps * 32, 0, st>>>(*w);
     if (any_dense) {
         const int n = w->n_kicks * S;
         wake_dense_kernel<<<(n + 127) / 128, 128, 0, st>>>(*w);

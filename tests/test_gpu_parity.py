@@ -109,6 +109,22 @@ def compare(rec, ref, label, rtol=RTOL, stat_rtol=1e-9, emit_rtol=1e-7,
             v = np.asarray(v, dtype=np.float64)
             g = np.asarray(g, dtype=np.float64)
             ok = np.isfinite(v)
+            # a slice with no more particles than coordinates in the
+            # emittance (x, x' and dp with dispersion; two without) has a
+            # singular covariance: its emittance is zero up to rounding,
+            # whose sign decides between a tiny value and NaN, on the GPU
+            # as in the reference -- only required to be tiny or NaN
+            if 'epsn' in k:
+                dim = 2 if (k.endswith('eff_epsn_x') or k.endswith('eff_epsn_y')
+                            or k.endswith('epsn_z')) else 3
+                turn, elem = k.split('_')[:2]
+                cnt = np.asarray(ref['%s_%s_counts' % (turn, elem)])
+                few = cnt <= dim
+                scale = np.max(np.abs(v[ok & ~few])) if np.any(ok & ~few) else 1.
+                gf = g[few]
+                assert np.all(~np.isfinite(gf) | (np.abs(gf) <= 1e-3 * scale)), \
+                    (label, k, gf)
+                ok &= ~few
             tol = (rtol if 'mean' in k else
                    emit_rtol if 'epsn' in k else stat_rtol)
             e = rms_err(g[ok], v[ok])
