@@ -302,8 +302,38 @@ def profile_traffic(kernel_key):
     return d.get(kernel_key)
 
 
-def time_form(w, coords, precision, steps, warmup, flush):
-    """Device time per turn (graph replay), track-kernel time, e2e."""
+def last_launch():
+    """Kernel, ring stages and shared memory of the last fused pass."""
+    import ctypes
+    from pyheadtail_gb300 import _native as N
+    v, s, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    N.call('phk_last_track_launch', ctypes.byref(v), ctypes.byref(s),
+           ctypes.byref(m))
+    return {'kernel': 'phk::stream_kernel' if v.value == 1
+            else 'phk::track_kernel', 'stages': s.value,
+            'smem_bytes': m.value}
+
+
+def time_form(w, coords, precision, steps, warmup, flush, tune=False):
+    """Device time per turn (graph replay), track-kernel time, e2e.
+    tune: time the launch plans of the FP32 pass first (its winner is
+    the plan the turn is captured with)."""
+    import tempfile
+    from pyheadtail_gb300 import _native as N
+    from pyheadtail_gb300 import tuning
+    tune = tune and precision == 'fp32'
+    if tune:
+        tuning.enable(cache_path=os.path.join(tempfile.mkdtemp(),
+                                              'plans.json'))
+    try:
+        return _time_form(w, coords, precision, steps, warmup, flush, tune)
+    finally:
+        if tune:
+            tuning.enable(on=False)
+            N.call('phk_set_track_plan', -1, -1, -1)
+
+
+def _time_form(w, coords, precision, steps, warmup, flush, tune):
     import torch
     from pyheadtail_gb300 import _native as N
     from pyheadtail_gb300.turngraph import StreamedTurns, TurnGraph
@@ -357,6 +387,7 @@ def time_form(w, coords, precision, steps, warmup, flush):
     evs = beam._engine.track_events
     beam._engine.track_events = None
     track_ms = [a.elapsed_time(b) for a, b in evs]
+    launch = dict(last_launch(), tuned=tune)
     # e2e: public API (turngraph.StreamedTurns), every step a bunch from
     # pinned host memory into a beam's coordinate arrays, one replay of its
     # captured turn(s), its centroid record read back; two beams take the
@@ -387,7 +418,8 @@ def time_form(w, coords, precision, steps, warmup, flush):
     return dict(graph_ms=graph_ms, turns_per_step=tpg,
                 e2e_turns_per_step=tg_turns, track_ms=track_ms,
                 e2e_s=e2e_s, h2d=h2d, d2h=8 * 34,
-                kernels_per_turn=kernels_per_turn, centroid=(cx, cy))
+                kernels_per_turn=kernels_per_turn, centroid=(cx, cy),
+                launch=launch)
 
 
 def cpu_baseline(w, coords, budget_s=12.0):
@@ -431,7 +463,8 @@ def run_ours(a, rank, world):
     for precision in ('fp64', 'fp32'):
         if a.form not in ('all', precision):
             continue
-        r = time_form(w, coords, precision, a.steps, a.warmup, flush)
+        r = time_form(w, coords, precision, a.steps, a.warmup, flush,
+                      tune=a.autotune)
         bytes_pp = 96 if precision == 'fp64' else 48
         step_ms = float(np.sum(r['graph_ms']))
         turns = a.steps * r['turns_per_step']
@@ -444,12 +477,13 @@ def run_ours(a, rank, world):
             'ms_per_step': step_ms / a.steps,
             'turns_per_step': r['turns_per_step'],
             'kernels_per_turn': r['kernels_per_turn'],
+            'launch_plan': r['launch'],
             'roofline': {'bound': 'hbm', 'achieved': achieved,
                          'peak': hbm_peak, 'unit': 'GB/s',
                          'frac': achieved / hbm_peak,
                          'peak_kind': peak_kind,
                          'traffic': None if tpp is None else tpp * w['n'],
-                         'kernel': 'phk::track_kernel',
+                         'kernel': r['launch']['kernel'],
                          'kernel_ms': track_avg,
                          'algorithmic_bytes_per_launch': bytes_pp * w['n']},
             'e2e': {'value': w['n'] * r['e2e_turns_per_step'] *
@@ -917,7 +951,8 @@ def main():
     ap.add_argument('--form', choices=['all', 'fp64', 'fp32'], default='all')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-autotune', dest='autotune', action='store_false',
-                    help='batched workload: skip timing the launch shapes')
+                    help='skip timing the launch shapes (FP32 pass, '
+                         'batched workload)')
     ap.add_argument('--stats-pass', action='store_true',
                     help='time the bunch statistics pass instead of the turn')
     a = ap.parse_args()

@@ -194,8 +194,14 @@ typedef struct phk_detuner {
 /* status (optional, device int32): a kernel that gives up a bounded wait
  * (a bulk copy that never completed) stores PHK_DEV_TIMEOUT there, stops
  * processing, drains its copies in flight and returns; the caller reads
- * it after synchronising.  NULL: no report. */
+ * it after synchronising.  If a drain wait gives up as well (default
+ * limit), the kernel stores PHK_DEV_TIMEOUT_UNDRAINED instead and returns
+ * with a copy or tensor-core operation possibly still in flight: the
+ * results of that launch and of later launches in the process are not to
+ * be trusted, and the caller should stop using the device from this
+ * process.  NULL: no report. */
 #define PHK_DEV_TIMEOUT 1
+#define PHK_DEV_TIMEOUT_UNDRAINED 4
 typedef struct phk_program {
     int32_t n_ops;
     int32_t n_det;
@@ -400,12 +406,34 @@ int phk_abi_version(void);
 
 /* Polls of a kernel's wait for its own bulk copies or tensor-core MMAs
  * before it gives up, stores PHK_DEV_TIMEOUT in its status word, waits
- * (with the default limit) for what it has in flight and returns.  polls < 0
+ * (with the default limit) for what it has in flight and returns; if that
+ * drain gives up too, the status is PHK_DEV_TIMEOUT_UNDRAINED.  polls < 0
  * restores the default (2^22 polls, of the order of a second); 0 makes every
  * such wait give up at once, which exercises the failure path without any
  * fault.  Process-wide; applies to launches made after the call.  No
  * counterpart in the reference (its kernels have no waits). */
 int phk_set_wait_limit(int64_t polls);
+
+/* Launch plan of the FP32 form's single-bunch pass (phk_track with float
+ * coordinates), process-wide, for launches made after the call: variant 0
+ * runs the tile-shared kernel, 1 the streaming kernel (one TMA ring per
+ * warp; used where the program is a transverse segment with or without
+ * RFSystems / LinearMap, or no element, with summed dipolar kicks), -1
+ * the default (the tile-shared kernel); stages: TMA ring stages (0, 2, 3
+ * for the tile-shared kernel, 2..4 for the streaming one; -1 the largest
+ * that fits); smem_kb: shared memory a CTA may plan for (16..227 KB; -1:
+ * 54 KB, four CTAs per SM).  A plan that does not apply to a launch falls
+ * back to the default for it.  Results are identical whatever the plan.
+ * Used by the autotuner of the Python layer (pyheadtail_gb300.tuning); no
+ * counterpart in the reference. */
+int phk_set_track_plan(int32_t variant, int32_t stages, int32_t smem_kb);
+
+/* The kernel variant (0 tile-shared, 1 streaming), TMA ring stages and
+ * dynamic shared memory per CTA of the last single-bunch phk_track launch
+ * in this process (-1 before the first); lets a caller check that a plan
+ * was honoured.  No counterpart in the reference. */
+int phk_last_track_launch(int32_t *variant, int32_t *stages,
+                          int32_t *smem_bytes);
 
 /* Number of kernels the library has launched in this process (all
  * devices, all threads): lets a caller verify which work ran natively. */

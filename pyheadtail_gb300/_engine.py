@@ -24,6 +24,7 @@ import numpy as np
 import torch
 
 from . import _native as N
+from . import tuning
 
 _F64, _F32 = N.PHK_F64, N.PHK_F32
 
@@ -347,6 +348,7 @@ class Engine(object):
             ev = (torch.cuda.Event(enable_timing=True),
                   torch.cuda.Event(enable_timing=True))
             ev[0].record()
+        self._set_plan(prog, coords, ks, ac, self.ops, self.kick, acc)
         N.call('phk_track', ctypes.byref(prog), ctypes.byref(coords),
                ctypes.byref(ks) if ks is not None else None,
                ctypes.byref(ac) if ac is not None else None, stream_handle())
@@ -359,12 +361,23 @@ class Engine(object):
         self.ops = []
         self.kick = None
 
+    def _set_plan(self, prog, coords, ks, ac, ops, kick, acc):
+        """With tuning on (pyheadtail_gb300.tuning), set the tuned launch
+        plan of this FP32 pass; otherwise leave the process's plan as it
+        is (the default unless phk_set_track_plan changed it)."""
+        if self.beam._code != _F32 or not tuning.enabled():
+            return
+        plan = tuning.plan_for(self, prog, coords, ks, ac, ops, kick, acc,
+                               stream_handle())
+        N.call('phk_set_track_plan', *plan)
+
     def slice_pass(self, acc):
         """Slicing pass over the coordinates as they are in memory, leaving
         any pending program and kick pending (z is not affected by kicks)."""
         prog = self.program_struct([])
         coords = self.coords_struct()
         ac = acc.struct()
+        self._set_plan(prog, coords, None, ac, [], None, acc)
         N.call('phk_track', ctypes.byref(prog), ctypes.byref(coords), None,
                ctypes.byref(ac), stream_handle())
         self.launches += 1

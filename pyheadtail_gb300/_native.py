@@ -12,6 +12,7 @@ from . import _build
 
 PHK_F64, PHK_F32 = 0, 1
 PHK_DEV_TIMEOUT = 1
+PHK_DEV_TIMEOUT_UNDRAINED = 4
 PHK_DEV_BAD_TABLE = 2
 PHK_MAX_OPS = 12
 PHK_MAX_DETUNERS = 6
@@ -181,6 +182,8 @@ SIGNATURES = {
                          ctypes.POINTER(ctypes.c_int64),
                          ctypes.POINTER(ctypes.c_int64)],
     'phk_wake_tc_expand': [ctypes.POINTER(WakeTC), ctypes.c_void_p],
+    'phk_set_track_plan': [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
+    'phk_last_track_launch': [ctypes.POINTER(ctypes.c_int32)] * 3,
     'phk_wake_tc_run': [ctypes.POINTER(WakeTC), ctypes.c_void_p],
     'phk_slice_noalloc': [ctypes.POINTER(Slicer), ctypes.POINTER(Coords),
                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

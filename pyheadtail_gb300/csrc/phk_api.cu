@@ -23,6 +23,20 @@ static std::atomic<unsigned> g_wait_limit(kDefaultWaitLimit);
 
 unsigned wait_limit() { return g_wait_limit.load(); }
 
+static std::atomic<int> g_plan_variant(-1), g_plan_stages(-1), g_plan_kb(-1);
+
+TrackPlan track_plan() {
+    return TrackPlan{g_plan_variant.load(), g_plan_stages.load(), g_plan_kb.load()};
+}
+
+static std::atomic<int> g_last_variant(-1), g_last_stages(-1), g_last_smem(-1);
+
+void note_track_launch(int variant, int stages, size_t smem) {
+    g_last_variant.store(variant);
+    g_last_stages.store(stages);
+    g_last_smem.store((int)smem);
+}
+
 int set_error(int code, const char* fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -180,6 +194,28 @@ int phk_set_wait_limit(int64_t polls) {
     g_wait_limit.store(polls < 0 ? kDefaultWaitLimit
                                  : (unsigned)(polls > 0xffffffffLL ? 0xffffffffLL
                                                                   : polls));
+    return PHK_OK;
+}
+
+int phk_set_track_plan(int32_t variant, int32_t stages, int32_t smem_kb) {
+    if (variant < -1 || variant > 1)
+        return set_error(PHK_EPARAM, "phk_set_track_plan: variant %d", variant);
+    if (stages < -1 || stages > 4 || stages == 1)
+        return set_error(PHK_EPARAM, "phk_set_track_plan: stages %d", stages);
+    if (smem_kb != -1 && (smem_kb < 16 || smem_kb > 227))
+        return set_error(PHK_EPARAM, "phk_set_track_plan: smem_kb %d", smem_kb);
+    g_plan_variant.store(variant);
+    g_plan_stages.store(stages);
+    g_plan_kb.store(smem_kb);
+    return PHK_OK;
+}
+
+int phk_last_track_launch(int32_t* variant, int32_t* stages, int32_t* smem_bytes) {
+    if (!variant || !stages || !smem_bytes)
+        return set_error(PHK_ENULL, "phk_last_track_launch: null pointer");
+    *variant = g_last_variant.load();
+    *stages = g_last_stages.load();
+    *smem_bytes = g_last_smem.load();
     return PHK_OK;
 }
 

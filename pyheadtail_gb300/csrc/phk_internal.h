@@ -17,6 +17,17 @@ void count_launches(int n);
 constexpr unsigned kDefaultWaitLimit = 1u << 22;
 unsigned wait_limit();
 
+// launch plan of the FP32 single-bunch pass (phk_set_track_plan): kernel
+// variant (-1 default, 0 track_kernel, 1 streaming kernel), TMA ring stages
+// (-1 default) and shared-memory budget per CTA in KB (-1 default)
+struct TrackPlan {
+    int variant, stages, smem_kb;
+};
+TrackPlan track_plan();
+// records the kernel variant, ring stages and shared memory of the last
+// single-bunch pass launched (phk_last_track_launch)
+void note_track_launch(int variant, int stages, size_t smem);
+
 // thread-local error message, read back by phk_last_error()
 int set_error(int code, const char* fmt, ...);
 

@@ -19,8 +19,6 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
-#include <mutex>
-
 #include "phk_internal.h"
 
 namespace phk {
@@ -31,28 +29,18 @@ constexpr int kNoAllocMaxColumns = 128;
 static __device__ __align__(256) double
     g_noalloc_partials[3 * kNoAllocMaxSlices * kNoAllocMaxColumns];
 
-// Device address of g_noalloc_partials on the current device, looked up once
-// per device with that device current (the host-side symbol is only a
-// stand-in and must never be passed to a kernel).
+// Device address of g_noalloc_partials in the current device's context,
+// looked up on every call (a cached address would go stale when the context
+// is destroyed and recreated, and the lookup costs far less than the pass).
+// The host-side symbol is only a stand-in and must never reach a kernel.
 static double* noalloc_scratch() {
-    static std::mutex mu;
-    static double* addr[64] = {nullptr};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess || !p) {
         cudaGetLastError();
         return nullptr;
     }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return nullptr;
-        }
-        addr[dev] = static_cast<double*>(p);
-    }
-    return addr[dev];
+    return static_cast<double*>(p);
 }
 
 }  // namespace phk

@@ -1698,11 +1698,15 @@ track_kernel(const __grid_constant__ phk_program prog,
             // has exited (earlier ones completed before their stage was
             // released)
             if (tid == 0) {
-                if (prog.status) atomicMax(prog.status, PHK_DEV_TIMEOUT);
+                bool drained = true;
                 for (int q = 0; q < a.stages; ++q)
-                    if (s_last[q] >= 0)
-                        mbar_wait(bars + q, (unsigned)((s_last[q] / a.stages) & 1),
-                                  kWaitLimit);
+                    if (s_last[q] >= 0 &&
+                        !mbar_wait(bars + q, (unsigned)((s_last[q] / a.stages) & 1),
+                                   kWaitLimit))
+                        drained = false;
+                if (prog.status)
+                    atomicMax(prog.status, drained ? PHK_DEV_TIMEOUT
+                                                   : PHK_DEV_TIMEOUT_UNDRAINED);
             }
             __syncthreads();
         } else if (has_partial) {
@@ -1834,17 +1838,29 @@ track_kernel(const __grid_constant__ phk_program prog,
 // whenever possible.  n_tables: kick tables staged per CTA.
 template <typename T>
 static size_t smem_for(int Sa, int Sp, int n_tables, bool tma, int* n_hist,
-                       int* kicks_smem, int* stages) {
+                       int* kicks_smem, int* stages, size_t budget_in = 0,
+                       int forced_stages = -1) {
     constexpr bool fix = sizeof(T) == 4;
     const int warps = kTrackThreads / 32;
     const int tile = kTrackThreads * (sizeof(T) == 8 ? 2 : kF32Vec);
-    const size_t budget = sizeof(T) == 8 ? kF64SmemBudget : kF32SmemBudget;
+    const size_t budget = budget_in ? budget_in
+                                    : (sizeof(T) == 8 ? kF64SmemBudget : kF32SmemBudget);
     *kicks_smem = n_tables > 0 && (size_t)n_tables * Sp * sizeof(T) <= 48 * 1024;
     const int hist_opts[4] = {warps, 4, 2, 1};
     const int n_hist_opts = fix ? 1 : 4;
     // ring stages (0: plain loads, the fallback for large slice counts)
     const int stage_opts[3] = {3, 2, 0};
     size_t off[9];
+    if (tma && (forced_stages == 0 || forced_stages == 2 || forced_stages == 3)) {
+        const int nh = 1;
+        const size_t b = track_smem_layout<T>(Sa, Sp, nh, n_tables, *kicks_smem,
+                                              forced_stages, tile, off, fix);
+        if (fix && b <= budget) {
+            *n_hist = nh;
+            *stages = forced_stages;
+            return b;
+        }
+    }
     size_t smallest = 0;
     for (int hi = 0; hi < n_hist_opts; ++hi) {
         for (int si = 0; si < (tma ? 3 : 1); ++si) {
@@ -2003,8 +2019,12 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     const bool tma = VEC > 1 && sizeof(T) == 4;
     plan_kick_tables<T>(pk, &a);
     int kicks_smem = 0;
-    const size_t smem = smem_for<T>(Sa, Sp, a.n_tables, tma, &a.n_hist,
-                                    &kicks_smem, &a.stages);
+    const TrackPlan pl = track_plan();
+    const bool planned = sizeof(T) == 4;
+    const size_t smem = smem_for<T>(
+        Sa, Sp, a.n_tables, tma, &a.n_hist, &kicks_smem, &a.stages,
+        planned && pl.smem_kb > 0 ? (size_t)pl.smem_kb * 1024 : 0,
+        planned ? pl.stages : -1);
     if (kicks_smem != a.kicks_smem)
         return set_error(PHK_EPARAM, "phk_track: inconsistent kick-table plan");
     if (smem > track_dynamic_smem_limit<T, VEC, SHAPE>())
@@ -2041,6 +2061,7 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     if (e != cudaSuccess)
         return set_error(PHK_ECUDA, "phk_track launch: %s", cudaGetErrorString(e));
     count_launches(1);
+    note_track_launch(0, a.stages, smem);
     return PHK_OK;
 }
 

@@ -343,7 +343,7 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
     // done; bounded)
     if (tid == 0) {
         umma_commit(fin);
-        if (!mbar_wait(fin, 0, kTcWaitLimit)) s_fail = 1;
+        if (!mbar_wait(fin, 0, kTcWaitLimit)) s_fail = 2;
     }
     tc_fence_before_sync();
     __syncthreads();
@@ -368,7 +368,10 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
             w.partials[((int64_t)sp * nk + k) * rows + row] = v;
         }
     }
-    if (s_fail && tid == 0 && w.status) atomicMax(w.status, PHK_DEV_TIMEOUT);
+    // 1: a stage wait gave up and every MMA issued completed; 2: the final
+    // wait for them gave up as well
+    if (s_fail && tid == 0 && w.status)
+        atomicMax(w.status, s_fail == 2 ? PHK_DEV_TIMEOUT_UNDRAINED : PHK_DEV_TIMEOUT);
     tc_fence_before_sync();
     __syncthreads();
     if (warp == 0) tmem_dealloc(taddr, 32);

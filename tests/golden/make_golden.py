@@ -4,7 +4,7 @@ Run in a container where the reference source tree is present (it is read
 only, so it is copied and its one Cython extension is built in a scratch
 directory first):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <PyHEADTAIL source tree>
 
 For every case in ``cases.py`` the script draws the seeded bunch with the
 reference's own generator (``ParticleGenerator`` + ``gaussian2D`` /
@@ -225,7 +225,8 @@ def run_case(name, spec):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', required=True,
+                    help='PyHEADTAIL source tree (read only)')
     ap.add_argument('--scratch', default='/tmp/phk_refbuild')
     ap.add_argument('cases', nargs='*')
     a = ap.parse_args()

@@ -4,7 +4,7 @@ machine, RF h=7 in its non-linear mode, parallel horizontal plates resistive
 wall, UniformChargeSlicer(500, n_sigma_z=3), 1000 turns, vertical growth
 rate 70e-4 per turn within 5 %), made by running PyHEADTAIL itself:
 
-    python tests/golden/make_golden_reswall.py [--ref /root/reference]
+    python tests/golden/make_golden_reswall.py --ref <PyHEADTAIL source tree>
 
 The bunch is the reference's RF-bucket-matched Gaussian (5e4 particles,
 numpy seed 2), rounded to float32 so that the fixture stays small; the
@@ -40,7 +40,8 @@ def machine_parameters():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', required=True,
+                    help='PyHEADTAIL source tree (read only)')
     ap.add_argument('--scratch', default='/tmp/pyht_ref')
     a = ap.parse_args()
     MG.build_reference(a.ref, a.scratch)

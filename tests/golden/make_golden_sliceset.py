@@ -3,7 +3,7 @@
 pidx_begin / pidx_end, lambda_bins, lambda_prime_bins, lambda_z,
 lambda_prime_z), made by running PyHEADTAIL itself on a seeded bunch:
 
-    python tests/golden/make_golden_sliceset.py [--ref /root/reference]
+    python tests/golden/make_golden_sliceset.py --ref <PyHEADTAIL source tree>
 
 Writes tests/golden/sliceset/analysis.npz (a subdirectory, apart from
 the turn-loop fixtures that the parity tests collect): the slicing (z_bins, slice index
@@ -24,7 +24,8 @@ import make_golden as MG  # noqa: E402
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', required=True,
+                    help='PyHEADTAIL source tree (read only)')
     ap.add_argument('--scratch', default='/tmp/pyht_ref')
     a = ap.parse_args()
     MG.build_reference(a.ref, a.scratch)

@@ -1,6 +1,6 @@
 """Generate the Synchrotron fixtures by running the PyHEADTAIL reference.
 
-    python tests/golden/make_golden_synchrotron.py [--ref /root/reference]
+    python tests/golden/make_golden_synchrotron.py --ref <PyHEADTAIL source tree>
 
 For every entry of cases.SYNCHROTRON_CASES: build the reference's
 Synchrotron, draw the seeded bunch with its generate_6D_Gaussian_bunch,
@@ -68,7 +68,8 @@ def run(name, spec):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', required=True,
+                    help='PyHEADTAIL source tree (read only)')
     ap.add_argument('--scratch', default='/tmp/phk_refbuild')
     ap.add_argument('cases', nargs='*')
     a = ap.parse_args()

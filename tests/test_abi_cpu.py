@@ -285,3 +285,55 @@ def test_fp32_fast_bin_path_random_slicers():
         assert np.array_equal(k[ok], want[ok].astype(np.int64)), (tail, head, S)
         taken += int(ok.sum())
     assert taken > 0
+
+
+def test_header_constants_match_binding():
+    """Every status, dtype and size constant of the header has the same
+    value in the Python binding."""
+    from pyheadtail_gb300 import _native as N
+    src = open(HEADER).read()
+    defs = dict(re.findall(r'#define\s+(PHK_\w+)\s+\(?(-?\d+)\)?', src))
+    for name in ('PHK_F64', 'PHK_F32', 'PHK_DEV_TIMEOUT',
+                 'PHK_DEV_TIMEOUT_UNDRAINED', 'PHK_DEV_BAD_TABLE',
+                 'PHK_MAX_OPS', 'PHK_MAX_DETUNERS', 'PHK_MAX_POLY',
+                 'PHK_MAX_KICKS', 'PHK_MAX_SLICES', 'PHK_X', 'PHK_DP'):
+        assert int(defs[name]) == getattr(N, name), name
+    # device status values are distinct
+    st = [int(defs[k]) for k in ('PHK_DEV_TIMEOUT', 'PHK_DEV_TIMEOUT_UNDRAINED',
+                                 'PHK_DEV_BAD_TABLE')]
+    assert len(set(st)) == 3
+
+
+def test_track_plan_validation(lib):
+    """phk_set_track_plan rejects out-of-range plans on the host and
+    accepts the tuner's candidates; phk_last_track_launch reports -1
+    before any launch in a process that has launched nothing."""
+    from pyheadtail_gb300 import _native as N
+    from pyheadtail_gb300 import tuning
+    L = N.load(build_if_missing=False)
+    for bad in ((2, -1, -1), (-2, -1, -1), (0, 1, -1), (0, 5, -1),
+                (1, -1, 15), (1, -1, 228)):
+        assert L.phk_set_track_plan(*bad) == -4, bad
+        assert 'phk_set_track_plan' in N.last_error()
+    for cand in tuning.CANDIDATES + [tuning.DEFAULT_PLAN]:
+        assert L.phk_set_track_plan(*cand) == 0, cand
+    assert L.phk_set_track_plan(-1, -1, -1) == 0
+    v, s, m = ctypes.c_int32(7), ctypes.c_int32(7), ctypes.c_int32(7)
+    assert L.phk_last_track_launch(ctypes.byref(v), ctypes.byref(s),
+                                   ctypes.byref(m)) == 0
+    assert L.phk_last_track_launch(None, ctypes.byref(s),
+                                   ctypes.byref(m)) == -1
+
+
+def test_tuning_disabled_leaves_plan_untouched(tmp_path):
+    """With tuning off the engine never sets a plan; the cache key names
+    the pass configuration."""
+    from pyheadtail_gb300 import tuning
+    assert not tuning.enabled()
+    tuning.enable(cache_path=str(tmp_path / 'p.json'))
+    try:
+        assert tuning.enabled()
+        assert tuning._load() == {}
+    finally:
+        tuning.enable(on=False)
+    assert not tuning.enabled()

@@ -79,8 +79,20 @@ def _errors():
     return e
 
 
-def test_fp32_form_errors_against_fp64_oracle():
-    e = _errors()
-    print('FP32 form errors after %d turns: %s' % (T, e))
+# launch plans of the FP32 pass (phk_set_track_plan: variant, ring
+# stages, shared-memory budget in KB): the default, the streaming kernel,
+# and the tile-shared kernel with fixed stages and a larger budget
+PLANS = [(-1, -1, -1), (1, -1, -1), (1, 4, 96), (0, 2, 72), (0, 0, -1)]
+
+
+@pytest.mark.parametrize('plan', PLANS, ids=lambda p: 'plan%d_%d_%d' % p)
+def test_fp32_form_errors_against_fp64_oracle(plan):
+    from pyheadtail_gb300 import _native as N
+    N.call('phk_set_track_plan', *plan)
+    try:
+        e = _errors()
+    finally:
+        N.call('phk_set_track_plan', -1, -1, -1)
+    print('FP32 form errors after %d turns, plan %s: %s' % (T, plan, e))
     for k, bar in BARS.items():
         assert e[k] <= bar, (k, e)

@@ -54,8 +54,19 @@ def _fp64_means(beam, S, q):
     return counts, np.where(counts > 0, sums / np.maximum(counts, 1), 0.)
 
 
+@pytest.fixture(params=[(-1, -1, -1), (1, -1, -1)],
+                ids=['tile_kernel', 'streaming_kernel'])
+def plan(request):
+    """Launch plan of the FP32 pass (phk_set_track_plan): the default
+    tile-shared kernel and the streaming kernel."""
+    from pyheadtail_gb300 import _native as N
+    N.call('phk_set_track_plan', *request.param)
+    yield request.param
+    N.call('phk_set_track_plan', -1, -1, -1)
+
+
 @pytest.mark.parametrize('n,S', [(10**7, 500), (5 * 10**7, 1000)])
-def test_repeated_slicing_bit_identical_and_exact(n, S):
+def test_repeated_slicing_bit_identical_and_exact(n, S, plan):
     import gpu_cases as G
     import cases as C
     beam = G.make_beam(C.beam_params(n, 0), _random_coords(n, 0),
@@ -81,7 +92,7 @@ def test_repeated_slicing_bit_identical_and_exact(n, S):
         assert err <= 2.0**-27 * umax * (1 + 1e-9), (q, err, umax)
 
 
-def test_turns_of_two_equal_beams_bit_identical():
+def test_turns_of_two_equal_beams_bit_identical(plan):
     """Two turns of the large-bunch physics (Q' = 2, amplitude detuning,
     RF, 1000 slices, resonator + 50-turn resistive wall) on two beams made
     from the same coordinates: identical slice sums and coordinates."""
