@@ -137,7 +137,9 @@ def build_gpu(w, coords, precision):
                                                                  RFSystems)
     from pyheadtail_gb300.trackers.transverse_tracking import TransverseMap
     sp = SilentPrinter()
-    beam = Particles(w['n'], 2.5e11 / w['n'], e, m_p, C_RING, GAMMA,
+    # a shard of the bunch holds part of its particles at the bunch's
+    # charge per macroparticle
+    beam = Particles(len(coords['x']), 2.5e11 / w['n'], e, m_p, C_RING, GAMMA,
                      coords_n_momenta_dict=coords, precision=precision)
     dets = []
     if w['chroma']:
@@ -527,6 +529,80 @@ def run_ours(a, rank, world):
     print(json.dumps(out))
 
 
+# ------------------------------------------------------ sharded bunch arm
+
+def run_sharded(a, rank, world):
+    """One bunch split over the ranks by particles (pyheadtail_gb300.shards):
+    every rank tracks its shard; the slice sums are all-gathered and
+    merged in rank order every turn; the wake is computed on every rank.
+    Eager turns (the all-gather is not captured in a graph); total work
+    fixed as N grows (strong scaling)."""
+    import torch
+    from pyheadtail_gb300 import shards as SH
+    w = WORKLOADS[a.workload]
+    coords = bunch_coords(w)
+    sh = SH.Shards()
+    lo, hi = sh.range(w['n'])
+    part = {k: np.ascontiguousarray(v[lo:hi]) for k, v in coords.items()}
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32,
+                        device='cuda')
+    sampler = ClockSampler(torch.cuda.current_device())
+    forms = {}
+    sampler.start()
+    for precision in ('fp64', 'fp32'):
+        if a.form not in ('all', precision):
+            continue
+        beam, elements = build_gpu(w, part, precision)
+        SH.shard(beam, sh)
+        for _ in range(max(a.warmup, w['rw_turns'] + 2, 3)):
+            for m in elements:
+                m.track(beam)
+        torch.cuda.synchronize()
+        ms = []
+        for i in range(a.steps):
+            flush_l2(flush)
+            if world > 1:
+                import torch.distributed as dist
+                dist.barrier()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for m in elements:
+                m.track(beam)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        step = max_over_ranks(float(np.mean(ms)), world)
+        forms[precision] = {'value': w['n'] / (step * 1e-3),
+                            'ms_per_step': step, 'turns_per_step': 1,
+                            'shard_macroparticles': hi - lo}
+        del beam, elements
+        torch.cuda.empty_cache()
+    clocks = sampler.stop()
+    if rank != 0:
+        return
+    prec = 'fp64' if 'fp64' in forms else 'fp32'
+    head = forms[prec]
+    print(json.dumps({
+        'metric': 'macroparticle-turns/s of one bunch sharded over the '
+                  'GPUs',
+        'value': head['value'], 'unit': 'macroparticle-turns/s',
+        'n_gpus': world, 'steps': a.steps, 'warmup': a.warmup,
+        'ms_per_step': head['ms_per_step'], 'higher_is_better': True,
+        'scaling': 'strong', 'vs_baseline': None,
+        'dtype': 'f64' if prec == 'fp64' else 'f32',
+        'data': 'synthetic: seeded 6D Gaussian bunch (reference generator '
+                'draw order), no dataset',
+        'config': bench_config(w), 'form': prec, 'turns_per_step': 1,
+        'timing': 'CUDA events around eager turns, max over ranks; L2 '
+                  'flushed between turns',
+        'parallelism': 'sharded single bunch: particles split over %d '
+                       'ranks, slice sums all-gathered and merged in rank '
+                       'order every turn, wake replicated' % world,
+        'clocks': clocks, 'forms': forms}))
+
+
 # ------------------------------------------------------------ batched arm
 
 def c4_draws():
@@ -578,13 +654,15 @@ def c4_bunch(n, q, intensity, coords, precision):
     return beam, list(tm) + [rf, wf]
 
 
-def time_batch(precision, steps, warmup, flush, autotune):
+def time_batch(precision, steps, warmup, flush, autotune, bunches=None):
+    """bunches: indices of the train's bunches this rank tracks (all by
+    default)."""
     import torch
     from pyheadtail_gb300 import _native as N
     from pyheadtail_gb300.batch import BatchedTurn, BunchBatch
     sizes, chroma, intensity = c4_draws()
     beams, maps = [], []
-    for b in range(len(sizes)):
+    for b in (range(len(sizes)) if bunches is None else bunches):
         c = c4_coords(int(sizes[b]), b, precision)
         beam, els = c4_bunch(int(sizes[b]), float(chroma[b]),
                              float(intensity[b]), c, precision)
@@ -740,10 +818,17 @@ def run_batch(a, rank, world):
     sampler = ClockSampler(dev)
     forms = {}
     sampler.start()
+    bunches = None
+    if a.shard:
+        # the train's bunches packed over the ranks (whole bunches, no
+        # exchange)
+        from pyheadtail_gb300.shards import pack_bunches
+        bunches = pack_bunches(c4_draws()[0], world)[rank]
     for precision in ('fp32', 'fp64'):
         if a.form not in ('all', precision):
             continue
-        r = time_batch(precision, steps, a.warmup, flush, a.autotune)
+        r = time_batch(precision, steps, a.warmup, flush, a.autotune,
+                       bunches)
         bytes_pp = 96 if precision == 'fp64' else 48
         n = r['particles']
         step_ms = float(np.sum(r['graph_ms']))
@@ -774,28 +859,35 @@ def run_batch(a, rank, world):
     prec = 'fp32' if 'fp32' in forms else 'fp64'
     head = forms[prec]
     ms_max = max_over_ranks(head['ms_per_step'], world)
+    total = head['particles']
+    if a.shard:
+        total = int(c4_draws()[0].sum())
     if rank != 0:
         return
     out = {
         'metric': 'macroparticle-turns/s on 1 GB300: FP32/batched vs FP64 '
                   'plain; % HBM roofline',
-        'value': job_value(head['particles'], ms_max, world),
+        'value': (total / (ms_max * 1e-3) if a.shard else
+                  job_value(head['particles'], ms_max, world)),
         'unit': 'macroparticle-turns/s',
         'n_gpus': world, 'steps': steps, 'warmup': a.warmup,
         'ms_per_step': ms_max,
-        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'higher_is_better': True,
+        'scaling': 'strong' if a.shard else 'weak', 'vs_baseline': None,
         'dtype': 'f32' if prec == 'fp32' else 'f64',
         'data': 'synthetic: 256 seeded matched Gaussian bunches drawn on the '
                 'device, no dataset',
         'config': {'workload': C4['label'],
-                   'n_macroparticles': head['particles'],
+                   'n_macroparticles': total,
                    'n_bunches': C4['n_bunches'], 'n_slices': C4['slices'],
                    'form': 'batched ' + prec, 'turns_per_step': 1,
                    'l2': 'flushed between steps (512 MiB write + 256 MiB '
                          'read-back, untimed); working set larger than L2',
                    'timing': 'CUDA events around a CUDA-graph replay of the '
                              'batched turn; inputs resident in HBM',
-                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+                   'parallelism': ('bunches packed over %d ranks' % world
+                                   if a.shard else
+                                   'replicas' if world > 1 else 'single GPU')},
         'roofline': head['roofline'],
         'e2e': head['e2e'],
         'gpu_launches': head['kernels_per_turn'] * steps,
@@ -955,6 +1047,10 @@ def main():
                          'batched workload)')
     ap.add_argument('--stats-pass', action='store_true',
                     help='time the bunch statistics pass instead of the turn')
+    ap.add_argument('--shard', action='store_true',
+                    help='split one bunch over the GPUs (particles; slice '
+                         'sums merged every turn) instead of one replica '
+                         'per GPU')
     a = ap.parse_args()
     a.steps_given = any(x == '--steps' or x.startswith('--steps=')
                         for x in sys.argv[1:])
@@ -975,6 +1071,8 @@ def main():
         dist.barrier()
     if a.workload == 'c4':
         run_batch(a, rank, world)
+    elif a.shard:
+        run_sharded(a, rank, world)
     else:
         run_ours(a, rank, world)
     if world > 1:

@@ -471,6 +471,26 @@ int phk_track(const phk_program *program, const phk_coords *coords,
 int phk_slice_finalize(const phk_accum *acc, int32_t *counts, double *mean_x,
                        double *mean_y, double *moments_slot, void *stream);
 
+/* Sharded bunch (the particles of one bunch split over several GPUs, one
+ * phk_track per shard): the column sums of this shard's partials in
+ * compensated form, sums = double[2][3][S]: [0][q][s] the high and
+ * [1][q][s] the low part of the count (q = 0), sum x (1) and sum y (2) of
+ * slice s.  Replaces, per shard, the per-slice sums of the reference's
+ * slicing (particles/slicing.py:443-470, cobra_functions/stats.pyx:235-253)
+ * that a sharded bunch must combine across shards. */
+int phk_slice_sums(const phk_accum *acc, double *sums, void *stream);
+
+/* Rank-ordered merge of the compensated sums of n_shards shards (device
+ * double[n_shards][2][3][S], shard 0 first, e.g. gathered over the ranks
+ * with an all-gather) into the outputs of phk_slice_finalize.  The totals
+ * are the columns' sums to about 2^-106 of the largest partial sum, so the
+ * result does not depend on how the columns are split over shards (it
+ * equals one shard holding all columns except where an exact sum lies
+ * within that distance of a rounding boundary). */
+int phk_slice_merge(const double *sums, int32_t n_shards, int32_t n_slices,
+                    int32_t *counts, double *mean_x, double *mean_y,
+                    double *moments_slot, void *stream);
+
 /* Wake convolution of every kick of `w` (see phk_wake_set). */
 int phk_wake(const phk_wake_set *w, void *stream);
 

@@ -183,6 +183,10 @@ SIGNATURES = {
                          ctypes.POINTER(ctypes.c_int64)],
     'phk_wake_tc_expand': [ctypes.POINTER(WakeTC), ctypes.c_void_p],
     'phk_set_track_plan': [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
+    'phk_slice_sums': [ctypes.POINTER(Accum), ctypes.c_void_p, ctypes.c_void_p],
+    'phk_slice_merge': [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                        ctypes.c_void_p, ctypes.c_void_p],
     'phk_last_track_launch': [ctypes.POINTER(ctypes.c_int32)] * 3,
     'phk_wake_tc_run': [ctypes.POINTER(WakeTC), ctypes.c_void_p],
     'phk_slice_noalloc': [ctypes.POINTER(Slicer), ctypes.POINTER(Coords),

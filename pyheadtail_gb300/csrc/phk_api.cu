@@ -262,6 +262,31 @@ int phk_slice_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
                            (cudaStream_t)stream);
 }
 
+int phk_slice_sums(const phk_accum* acc, double* sums, void* stream) {
+    if (!acc || !sums)
+        return set_error(PHK_ENULL, "phk_slice_sums: acc or sums is NULL");
+    int r = check_accum(acc, "phk_slice_sums");
+    if (r) return r;
+    if (reinterpret_cast<uintptr_t>(sums) % 8)
+        return set_error(PHK_EALIGN, "phk_slice_sums: sums not 8-byte aligned");
+    return launch_slice_sums(acc, sums, (cudaStream_t)stream);
+}
+
+int phk_slice_merge(const double* sums, int32_t n_shards, int32_t n_slices,
+                    int32_t* counts, double* mean_x, double* mean_y,
+                    double* moments_slot, void* stream) {
+    if (!sums) return set_error(PHK_ENULL, "phk_slice_merge: sums is NULL");
+    if (n_shards < 1 || n_shards > 65536)
+        return set_error(PHK_ESIZE, "phk_slice_merge: n_shards %d", n_shards);
+    if (n_slices < 1 || n_slices > PHK_MAX_SLICES)
+        return set_error(PHK_ESIZE, "phk_slice_merge: n_slices %d outside "
+                         "[1, %d]", n_slices, PHK_MAX_SLICES);
+    if (reinterpret_cast<uintptr_t>(sums) % 8)
+        return set_error(PHK_EALIGN, "phk_slice_merge: sums not 8-byte aligned");
+    return launch_slice_merge(sums, n_shards, n_slices, counts, mean_x, mean_y,
+                              moments_slot, (cudaStream_t)stream);
+}
+
 int phk_wake(const phk_wake_set* w, void* stream) {
     if (!w) return set_error(PHK_ENULL, "phk_wake: wake set is NULL");
     if (w->n_slices < 1 || w->n_slices > PHK_MAX_SLICES)

@@ -47,6 +47,10 @@ int launch_track(const phk_program* prog, const phk_coords* c,
                  cudaStream_t stream);
 int track_grid(int64_t n, int32_t dtype, int32_t n_slices);
 size_t track_smem_bytes(int32_t dtype, int32_t acc_slices, int32_t pk_slices);
+int launch_slice_sums(const phk_accum* acc, double* out, cudaStream_t st);
+int launch_slice_merge(const double* sums, int n_shards, int S,
+                       int32_t* counts, double* mean_x, double* mean_y,
+                       double* moments, cudaStream_t st);
 int launch_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
                     double* mean_y, double* moments, cudaStream_t stream);
 int launch_wake(const phk_wake_set* w, cudaStream_t stream);

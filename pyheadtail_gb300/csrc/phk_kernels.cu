@@ -147,6 +147,130 @@ int launch_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
 }
 
 // ===================================================================
+// compensated column sums of a particle shard (one warp per slice)
+// ===================================================================
+
+// Error-free sum: s + e == a + b exactly (Knuth's TwoSum, six operations,
+// no branch); symmetric in a and b.
+__device__ __forceinline__ void two_sum(double a, double b, double* s,
+                                        double* e) {
+    const double t = add(a, b);
+    const double bb = sub(t, a);
+    *e = add(sub(a, sub(t, bb)), sub(b, bb));
+    *s = t;
+}
+
+// (hi, lo) pairs: hi the running sum, lo the running sum of the exact
+// rounding errors; combining two pairs adds their lows and the error of
+// the high sum.
+__device__ __forceinline__ void dd_combine(double& hi, double& lo, double bh,
+                                           double bl) {
+    double s, e;
+    two_sum(hi, bh, &s, &e);
+    lo = add(add(lo, bl), e);
+    hi = s;
+}
+
+// Per slice s and quantity q (count, sum x, sum y): lane l adds columns
+// l, l + 32, ... in order into its (hi, lo) pair, then the lanes combine
+// in a fixed butterfly (partner l ^ 16, ^ 8, ^ 4, ^ 2, ^ 1); lane 0 writes
+// out[(0 * 3 + q) * S + s] = hi, out[(1 * 3 + q) * S + s] = lo.  hi + lo
+// is the sum of the columns to about 2^-106 of the largest partial sum,
+// so sums of disjoint column sets merged the same way (phk_slice_merge on
+// the pairs of every shard) round to the same double as one fold over
+// all columns.
+__global__ void slice_sums_kernel(const double* __restrict__ P, int S, int G,
+                                  double* __restrict__ out) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= S) return;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double* pc = P + ((int64_t)q * S + warp) * G;
+        double hi = 0.0, lo = 0.0;
+        for (int g = lane; g < G; g += 32) {
+            double s, e;
+            two_sum(hi, pc[g], &s, &e);
+            hi = s;
+            lo = add(lo, e);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double bh = __shfl_xor_sync(0xffffffffu, hi, o);
+            const double bl = __shfl_xor_sync(0xffffffffu, lo, o);
+            dd_combine(hi, lo, bh, bl);
+        }
+        if (lane == 0) {
+            out[(int64_t)q * S + warp] = hi;
+            out[(int64_t)(3 + q) * S + warp] = lo;
+        }
+    }
+}
+
+int launch_slice_sums(const phk_accum* acc, double* out, cudaStream_t st) {
+    const int S = acc->slicer.n_slices;
+    const int threads = 256;
+    const int blocks = (S * 32 + threads - 1) / threads;
+    slice_sums_kernel<<<blocks, threads, 0, st>>>(acc->partials, S, acc->grid,
+                                                  out);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_slice_sums launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+// Rank-ordered merge of the (hi, lo) pairs of n_shards shards, laid out
+// [n_shards][2][3][S]: shard 0's pair, combined with shard 1's, then 2's,
+// ...; then the finalised outputs of phk_slice_finalize from the totals
+// hi + lo.  One thread per slice.
+__global__ void slice_merge_kernel(const double* __restrict__ sums,
+                                   int n_shards, int S, int32_t* counts,
+                                   double* mean_x, double* mean_y,
+                                   double* moments) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    double t[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        double hi = sums[(int64_t)q * S + s];
+        double lo = sums[(int64_t)(3 + q) * S + s];
+        for (int r = 1; r < n_shards; ++r) {
+            const double* b = sums + (int64_t)r * 6 * S;
+            dd_combine(hi, lo, b[(int64_t)q * S + s], b[(int64_t)(3 + q) * S + s]);
+        }
+        t[q] = add(hi, lo);
+    }
+    const int32_t n = (int32_t)t[0];
+    const double mx = n ? dvd(t[1], (double)n) : 0.0;
+    const double my = n ? dvd(t[2], (double)n) : 0.0;
+    if (counts) counts[s] = n;
+    if (mean_x) mean_x[s] = mx;
+    if (mean_y) mean_y[s] = my;
+    if (moments) {
+        moments[s] = (double)n;
+        moments[S + s] = mul((double)n, mx);
+        moments[2 * S + s] = mul((double)n, my);
+    }
+}
+
+int launch_slice_merge(const double* sums, int n_shards, int S,
+                       int32_t* counts, double* mean_x, double* mean_y,
+                       double* moments, cudaStream_t st) {
+    const int threads = 128;
+    const int blocks = (S + threads - 1) / threads;
+    slice_merge_kernel<<<blocks, threads, 0, st>>>(sums, n_shards, S, counts,
+                                                   mean_x, mean_y, moments);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return set_error(PHK_ECUDA, "phk_slice_merge launch: %s",
+                         cudaGetErrorString(e));
+    count_launches(1);
+    return PHK_OK;
+}
+
+// ===================================================================
 // wake convolution
 // ===================================================================
 

@@ -575,6 +575,13 @@ class UniformChargeSlicer(Slicer):
 def make_slice_set(slicer, beam, with_means=False, moments_out=None):
     """Flush the beam's pending program with a fused slicing pass and wrap
     the per-slice results in a SliceSet."""
+    shards = getattr(beam, '_shard', None)
+    if shards is not None and (slicer.mode == 'uniform_charge' or
+                               getattr(slicer, 'z_cuts', None) is None):
+        raise NotImplementedError(
+            'a sharded bunch needs a uniform-bin slicer with fixed z_cuts '
+            '(bunch-dependent cuts and uniform-charge slices need the whole '
+            "bunch's statistics)")
     tail, head = slicer.get_long_cuts(beam)
     eng = beam._engine
     if slicer.mode == 'uniform_charge':
@@ -596,12 +603,17 @@ def make_slice_set(slicer, beam, with_means=False, moments_out=None):
     if with_means or moments_out is not None:
         mx = torch.empty(S, dtype=torch.float64, device=dev)
         my = torch.empty(S, dtype=torch.float64, device=dev)
-    a = acc.struct()
-    N.call('phk_slice_finalize', __import__('ctypes').byref(a),
-           counts.data_ptr(), 0 if mx is None else mx.data_ptr(),
-           0 if my is None else my.data_ptr(),
-           0 if moments_out is None else moments_out.data_ptr(),
-           E.stream_handle())
+    if shards is not None:
+        from .. import shards as SH
+        SH.merged_slice_moments(beam, acc, counts, mx, my, moments_out,
+                                E.stream_handle())
+    else:
+        a = acc.struct()
+        N.call('phk_slice_finalize', __import__('ctypes').byref(a),
+               counts.data_ptr(), 0 if mx is None else mx.data_ptr(),
+               0 if my is None else my.data_ptr(),
+               0 if moments_out is None else moments_out.data_ptr(),
+               E.stream_handle())
     params = Slicer.extract_beam_parameters(beam)
     params['is_sorted'] = False
     ss = SliceSet(z_bins, slicer.mode, ds, beam, counts,
@@ -654,9 +666,15 @@ def add_statistics(ss, beam, statistics):
     """Slicer.add_statistics (slicing.py:443-529) for the GPU SliceSet."""
     if statistics is True:
         statistics = ALL_STATS
+    sh = getattr(beam, '_shard', None)
     for stat in statistics:
         if hasattr(ss, stat):
             continue
+        if sh is not None and sh.world > 1:
+            raise NotImplementedError(
+                'slice statistic %r of a sharded bunch: only the merged '
+                'mean_x and mean_y of its slicing are whole-bunch values'
+                % stat)
         if stat.startswith('mean_'):
             means, _, _ = _slice_moments(ss, beam, [_STAT_COORDS[stat]])
             setattr(ss, stat, means[0].clone())

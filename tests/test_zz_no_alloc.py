@@ -2,8 +2,8 @@
 library-owned device array, against the workspace entry points
 phk_track + phk_slice_finalize on the same inputs, called through the C ABI,
 and against an FP64 binning and summation on the host (the reference's
-formula, int(floor((z - tail) / width)), particles/slicing.py:604-611).  One case
-per dtype has more partial columns than the scratch array holds (the
+formula, int(floor((z - tail) / width)), particles/slicing.py:604-611).  The
+large FP32 case has more partial columns than the scratch array holds (the
 clamp to 128 columns, the kernel's tile loop covering the rest).
 
 The file sorts last so that its GPU test also runs after every other test
@@ -114,8 +114,9 @@ def test_no_alloc_matches_workspace_entry_point_twice(code, n, S,
     sl = DeviceSlicer(-0.69, 0.69, S, code, 'cuda')
     coords = _coords(x, y, z, code, with_momenta)
     stream = torch.cuda.current_stream().cuda_stream
-    if n >= 10_000_000:
-        # more partial columns than the library-owned array holds
+    if n >= 10_000_000 and code == 1:
+        # more partial columns than the library-owned array holds (the
+        # FP64 pass has fewer CTAs per SM: 74 clusters at this size)
         assert L.phk_track_grid(n, code, S) > 128
     ref_counts, ref_mx, ref_my = _with_workspace(L, sl, coords, stream)
     host_counts, host_mx, host_my = _host_reference(x, y, z, sl)
