@@ -390,6 +390,10 @@ def _time_form(w, coords, precision, steps, warmup, flush, tune):
     beam._engine.track_events = None
     track_ms = [a.elapsed_time(b) for a, b in evs]
     launch = dict(last_launch(), tuned=tune)
+    if tune:
+        from pyheadtail_gb300 import tuning
+        tuned = list(tuning.timings().values())
+        launch['candidates_ms'] = tuned[0].get('candidates') if tuned else None
     # e2e: public API (turngraph.StreamedTurns), every step a bunch from
     # pinned host memory into a beam's coordinate arrays, one replay of its
     # captured turn(s), its centroid record read back; two beams take the
@@ -448,6 +452,45 @@ def cpu_baseline(w, coords, budget_s=12.0):
             'sample': '%d macroparticles x %d turns of the same workload '
                       '(oracle: NumPy restatement of the reference, single '
                       'thread, like the reference)' % (ns, turns)}
+
+
+def run_eager(a):
+    """A short run for profilers: `a.eager_turns` eager turns of the
+    workload in each selected form (no graph, no timing loop), then the
+    track-kernel time of the last three turns and the bunch centroid."""
+    import tempfile
+    import torch
+    from pyheadtail_gb300 import tuning
+    w = WORKLOADS[a.workload]
+    coords = bunch_coords(w)
+    for precision in ('fp64', 'fp32'):
+        if a.form not in ('all', precision):
+            continue
+        if a.autotune and precision == 'fp32':
+            tuning.enable(cache_path=os.path.join(tempfile.mkdtemp(),
+                                                  'plans.json'))
+        beam, elements = build_gpu(w, coords, precision)
+        for t in range(a.eager_turns):
+            if t == a.eager_turns - 3:
+                beam._engine.track_events = []
+            for m in elements[:-1]:
+                m.track(beam)
+            if t >= a.eager_turns - 3:
+                # the GPU busy while the pass is launched: its events time
+                # the device only
+                torch.cuda._sleep(SPIN_CYCLES)
+            elements[-1].track(beam)
+        torch.cuda.synchronize()
+        evs = beam._engine.track_events or []
+        print(json.dumps({'form': precision, 'turns': a.eager_turns,
+                          'track_ms': [x.elapsed_time(y) for x, y in evs],
+                          'launch': last_launch(),
+                          'tuning': tuning.timings()
+                          if tuning.enabled() else None,
+                          'mean_x': float(beam.mean_x())}))
+        tuning.enable(on=False)
+        del beam, elements
+        torch.cuda.empty_cache()
 
 
 def run_ours(a, rank, world):
@@ -1051,6 +1094,13 @@ def main():
                     help='split one bunch over the GPUs (particles; slice '
                          'sums merged every turn) instead of one replica '
                          'per GPU')
+    ap.add_argument('--plan', default=None,
+                    help='variant,stages,smem_kb: launch plan of the FP32 '
+                         'pass (phk_set_track_plan) instead of the default '
+                         'or the tuned one')
+    ap.add_argument('--eager-turns', type=int, default=0,
+                    help='run this many eager turns of the workload and '
+                         'exit (a short run for profilers; no timing loop)')
     a = ap.parse_args()
     a.steps_given = any(x == '--steps' or x.startswith('--steps=')
                         for x in sys.argv[1:])
@@ -1059,6 +1109,12 @@ def main():
     rank = int(os.environ.get('RANK', '0'))
     if a.stats_pass and a.impl == 'ours':
         return run_stats_pass(a, rank, world)
+    if a.plan and a.impl == 'ours':
+        from pyheadtail_gb300 import _native as N
+        N.call('phk_set_track_plan', *[int(x) for x in a.plan.split(',')])
+        a.autotune = False
+    if a.eager_turns and a.impl == 'ours':
+        return run_eager(a)
     if a.impl == 'reference':
         if a.workload == 'c4':
             return run_reference_c4(a, rank, world)

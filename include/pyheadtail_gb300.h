@@ -422,7 +422,7 @@ int phk_set_wait_limit(int64_t polls);
  * the default (the tile-shared kernel); stages: TMA ring stages (0, 2, 3
  * for the tile-shared kernel, 2..4 for the streaming one; -1 the largest
  * that fits); smem_kb: shared memory a CTA may plan for (16..227 KB; -1:
- * 54 KB, four CTAs per SM).  A plan that does not apply to a launch falls
+ * 56 KB, four CTAs per SM).  A plan that does not apply to a launch falls
  * back to the default for it.  Results are identical whatever the plan.
  * Used by the autotuner of the Python layer (pyheadtail_gb300.tuning); no
  * counterpart in the reference. */

@@ -20,7 +20,12 @@ constexpr int kStreamWarps = 8;
 constexpr int kStreamThreads = kStreamWarps * 32;
 constexpr int kStreamTile = 64;          // particles per warp-tile
 constexpr int kStreamMaxStages = 4;
-constexpr size_t kStreamSmemBudget = 54 * 1024;
+constexpr size_t kStreamSmemBudget = 56 * 1024;
+#ifndef PHK_STREAM_WORDS
+#define PHK_STREAM_WORDS 0
+#endif
+// slice sums of the streaming kernel: FixWords (1) or FixHist (0)
+constexpr bool kStreamWords = PHK_STREAM_WORDS != 0;
 
 struct StreamArgs {
     float* c[6];
@@ -182,6 +187,150 @@ __device__ __forceinline__ void sp_program(const StreamProg& sp, Tile<float, 1>&
     }
 }
 
+// ---- the same element arithmetic for the lane's two particles on the
+// paired FP32 pipes (FFMA2 / FADD2 / FMUL2): every lane rounds as the scalar
+// forms above, operation for operation
+struct Pair {
+    float2 c[6];
+};
+
+__device__ __forceinline__ void sp_detune_x2(const StreamProg& sp, int d,
+                                             const Pair& t, float2& dqx,
+                                             float2& dqy) {
+    const float* c = sp.det[d];
+    const float2 DP = t.c[PHK_DP];
+    if (sp.det_kind[d] == PHK_DET_CHROMA) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int n = q ? sp.det_ny[d] : sp.det_nx[d];
+            const float* cq = c + 8 * q;
+            float2& dq = q ? dqy : dqx;
+            if (n == 1) dq = fma2(f2(cq[0]), DP, dq);
+            else if (n == 2) dq = fma2(fma2(f2(cq[1]), DP, f2(cq[0])), DP, dq);
+            else dq = fma2(fma2(fma2(f2(cq[2]), DP, f2(cq[1])), DP, f2(cq[0])), DP, dq);
+        }
+    } else {
+        const float2 X = t.c[PHK_X], XP = t.c[PHK_XP];
+        const float2 Y = t.c[PHK_Y], YP = t.c[PHK_YP];
+        const float2 Jx = mul2(f2(0.5f), fma2(mul2(f2(c[6]), XP), XP,
+                                              fma2(mul2(f2(c[5]), X), XP,
+                                                   mul2(mul2(f2(c[4]), X), X))));
+        const float2 Jy = mul2(f2(0.5f), fma2(mul2(f2(c[9]), YP), YP,
+                                              fma2(mul2(f2(c[8]), Y), YP,
+                                                   mul2(mul2(f2(c[7]), Y), Y))));
+        dqx = add2(dqx, fma2(f2(c[0]), Jx, mul2(f2(c[2]), Jy)));
+        dqy = add2(dqy, fma2(f2(c[1]), Jy, mul2(f2(c[3]), Jx)));
+    }
+}
+
+__device__ __forceinline__ void sp_transverse_x2(const StreamProg& sp, Pair& t) {
+    const float* p = sp.op[0];
+    const int f = sp.flags[0];
+    float2 X = t.c[PHK_X], XP = t.c[PHK_XP], Y = t.c[PHK_Y], YP = t.c[PHK_YP];
+    const float2 DP = t.c[PHK_DP];
+    float2 M[8];
+    const bool detuned = f & PHK_FLAG_DETUNED;
+    if (detuned) {
+        float2 dqx = f2(0.f), dqy = f2(0.f);
+        if (sp.n_det > 0) sp_detune_x2(sp, 0, t, dqx, dqy);
+        if (sp.n_det > 1) sp_detune_x2(sp, 1, t, dqx, dqy);
+        float2 sx, cx, sy, cy;
+        sincos_turns_x2(f2(p[16]), f2(p[17]), dqx, &sx, &cx);
+        sincos_turns_x2(f2(p[18]), f2(p[19]), dqy, &sy, &cy);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            M[e] = fma2(f2(p[e]), cx, fma2(f2(p[8 + e]), sx,
+                                           fma2(f2(p[40 + e]), cx, mul2(f2(p[48 + e]), sx))));
+            M[4 + e] = fma2(f2(p[4 + e]), cy, fma2(f2(p[12 + e]), sy,
+                                                   fma2(f2(p[44 + e]), cy, mul2(f2(p[52 + e]), sy))));
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) M[e] = f2(p[e]);
+    }
+    if (f & PHK_FLAG_DISPERSION) {
+        X = fma2(f2(-p[32]), DP, X);
+        Y = fma2(f2(-p[34]), DP, Y);
+    }
+    float2 cxr = f2(0.f), cxp = f2(0.f), cyr = f2(0.f), cyp = f2(0.f);
+    if (!detuned) {
+        cxr = fma2(f2(p[40]), X, mul2(f2(p[41]), XP));
+        cxp = fma2(f2(p[42]), X, mul2(f2(p[43]), XP));
+        cyr = fma2(f2(p[44]), Y, mul2(f2(p[45]), YP));
+        cyp = fma2(f2(p[46]), Y, mul2(f2(p[47]), YP));
+    }
+    const float2 nx = fma2(M[0], X, fma2(M[1], XP, cxr));
+    const float2 nxp = fma2(M[2], X, fma2(M[3], XP, cxp));
+    const float2 ny = fma2(M[4], Y, fma2(M[5], YP, cyr));
+    const float2 nyp = fma2(M[6], Y, fma2(M[7], YP, cyp));
+    X = nx; XP = nxp; Y = ny; YP = nyp;
+    if (f & PHK_FLAG_DISPERSION) {
+        X = fma2(f2(p[33]), DP, X);
+        Y = fma2(f2(p[35]), DP, Y);
+    }
+    t.c[PHK_X] = X; t.c[PHK_XP] = XP; t.c[PHK_Y] = Y; t.c[PHK_YP] = YP;
+}
+
+template <int OPI>
+__device__ __forceinline__ void sp_drift_x2(const StreamProg& sp, Pair& t) {
+    const float* p = sp.op[OPI];
+    const float2 Z = t.c[PHK_Z], DP = t.c[PHK_DP];
+    const float2 zs = (sp.flags[OPI] & PHK_FLAG_SHRINK)
+                          ? fma2(f2(p[0]), Z, mul2(f2(p[3]), Z)) : Z;
+    t.c[PHK_Z] = fma2(f2(-p[1]), DP, fma2(f2(-p[2]), DP, zs));
+}
+
+__device__ __forceinline__ void sp_rfkick_x2(const StreamProg& sp, Pair& t) {
+    const float* p = sp.op[2];
+    const bool disp = sp.flags[2] & PHK_FLAG_DISPERSION;
+    float2 DP = t.c[PHK_DP];
+    if (disp) {
+        t.c[PHK_X] = fma2(f2(-p[8]), DP, t.c[PHK_X]);
+        t.c[PHK_Y] = fma2(f2(-p[9]), DP, t.c[PHK_Y]);
+    }
+    const float2 s = sin_turns_of_product_x2(t.c[PHK_Z], p[0], p[1], p[2], p[3]);
+    DP = fma2(f2(p[4]), s, fma2(f2(p[10]), s,
+                                fma2(DP, f2(p[5]), fma2(DP, f2(p[11]), f2(-p[6])))));
+    t.c[PHK_DP] = DP;
+    if (disp) {
+        t.c[PHK_X] = fma2(f2(p[8]), DP, t.c[PHK_X]);
+        t.c[PHK_Y] = fma2(f2(p[9]), DP, t.c[PHK_Y]);
+    }
+}
+
+__device__ __forceinline__ void sp_linear_long_x2(const StreamProg& sp, Pair& t) {
+    const float* p = sp.op[1];
+    const bool disp = sp.flags[1] & PHK_FLAG_DISPERSION;
+    if (disp) {
+        t.c[PHK_X] = fma2(f2(-p[4]), t.c[PHK_DP], t.c[PHK_X]);
+        t.c[PHK_Y] = fma2(f2(-p[5]), t.c[PHK_DP], t.c[PHK_Y]);
+    }
+    const float2 z0 = t.c[PHK_Z], dp0 = t.c[PHK_DP];
+    t.c[PHK_Z] = fma2(z0, f2(p[0]), fma2(f2(-p[2]), dp0,
+                                         fma2(z0, f2(p[1]), mul2(f2(-p[3]), dp0))));
+    t.c[PHK_DP] = fma2(dp0, f2(p[0]), fma2(f2(p[6]), z0,
+                                           fma2(dp0, f2(p[1]), mul2(f2(p[7]), z0))));
+    if (disp) {
+        t.c[PHK_X] = fma2(f2(p[4]), t.c[PHK_DP], t.c[PHK_X]);
+        t.c[PHK_Y] = fma2(f2(p[5]), t.c[PHK_DP], t.c[PHK_Y]);
+    }
+}
+
+template <int SHAPE>
+__device__ __forceinline__ void sp_program_x2(const StreamProg& sp, Pair& t) {
+    if constexpr (SHAPE == SHAPE_T) {
+        sp_transverse_x2(sp, t);
+    } else if constexpr (SHAPE == SHAPE_T_RF) {
+        sp_transverse_x2(sp, t);
+        sp_drift_x2<1>(sp, t);
+        sp_rfkick_x2(sp, t);
+        sp_drift_x2<3>(sp, t);
+    } else if constexpr (SHAPE == SHAPE_T_LIN) {
+        sp_transverse_x2(sp, t);
+        sp_linear_long_x2(sp, t);
+    }
+}
+
 // coordinates a shape reads and writes (bit q = coordinate q)
 template <int SHAPE, bool PK, bool ACC>
 constexpr int stream_load_bits() {
@@ -197,8 +346,13 @@ __host__ __device__ inline size_t stream_smem_layout(int Sa, int Sp,
                                                      int n_tables, int stages,
                                                      size_t* off) {
     size_t b = 0;
-    off[0] = b; b = align16(b + (size_t)4 * Sa);
-    off[1] = b; b = align16(b + (size_t)4 * 6 * Sa);
+    if (kStreamWords) {
+        off[0] = b; b = align16(b + (size_t)8 * 2 * Sa);     // FixWords
+        off[1] = b;
+    } else {
+        off[0] = b; b = align16(b + (size_t)4 * Sa);          // FixHist count
+        off[1] = b; b = align16(b + (size_t)4 * 4 * Sa);      // digits
+    }
     off[2] = b; b = align16(b + (size_t)4 * ((Sa + 3) / 4));
     off[3] = b; b = align16(b + (size_t)4 * (Sa > 0 ? Sa + 1 : 0));
     off[4] = b; b = align16(b + (size_t)4 * (Sp > 0 ? Sp + 1 : 0));
@@ -215,13 +369,13 @@ constexpr int stream_store_bits() {
 }
 
 // pending kicks, program, accumulation of one particle
-template <int SHAPE, bool PK, bool ACC>
+template <int SHAPE, bool PK, bool ACC, typename F>
 __device__ __forceinline__ void stream_particle(const StreamProg& sp,
                                                 const StreamArgs& a,
                                                 const Bins<float>& bpk,
                                                 const Bins<float>& bac,
                                                 const float* ktab, int Sp,
-                                                const FixHist& fix,
+                                                const F& fix,
                                                 Tile<float, 1>& t) {
     if constexpr (PK) {
         const int s = bpk.index(t.c[PHK_Z][0]);
@@ -238,6 +392,58 @@ __device__ __forceinline__ void stream_particle(const StreamProg& sp,
     }
 }
 
+// the slice-sum accumulator's shared arrays and its periodic flush
+__device__ __forceinline__ void acc_bind(FixWords& f, unsigned long long* fw,
+                                         int*, int*) {
+    f.w = fw;
+}
+__device__ __forceinline__ void acc_bind(FixHist& f, unsigned long long*,
+                                         int* cnt, int* dig) {
+    f.cnt = cnt;
+    f.dig = dig;
+}
+__device__ __forceinline__ void acc_flush(const FixWords& f, long long* cnt,
+                                          int tid, int nthreads) {
+    fix_words_flush(f, cnt, tid, nthreads);
+}
+__device__ __forceinline__ void acc_flush(const FixHist& f, long long*,
+                                          int tid, int nthreads) {
+    fix_flush(f, tid, nthreads);
+}
+
+// pending kicks, program and accumulation of the lane's two particles
+template <int SHAPE, bool PK, bool ACC, typename F>
+__device__ __forceinline__ void stream_pair(const StreamProg& sp,
+                                            const StreamArgs& a,
+                                            const Bins<float>& bpk,
+                                            const Bins<float>& bac,
+                                            const float* ktab, int Sp,
+                                            const F& fix, Pair& t) {
+    if constexpr (PK) {
+        const float zv[2] = {t.c[PHK_Z].x, t.c[PHK_Z].y};
+        int sl[2];
+        bpk.index_vec<2>(zv, sl);
+        const bool on0 = sl[0] >= 0, on1 = sl[1] >= 0;
+        const int s0 = on0 ? sl[0] : 0, s1 = on1 ? sl[1] : 0;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int slot = a.comb_slot[q];
+            if (slot < 0) continue;
+            const float* tab = ktab + slot * Sp;
+            const int c = q == 0 ? PHK_XP : (q == 1 ? PHK_YP : PHK_DP);
+            t.c[c] = add2(t.c[c], make_float2(on0 ? tab[s0] : 0.f, on1 ? tab[s1] : 0.f));
+        }
+    }
+    sp_program_x2<SHAPE>(sp, t);
+    if constexpr (ACC) {
+        const float zv[2] = {t.c[PHK_Z].x, t.c[PHK_Z].y};
+        int sl[2];
+        bac.index_vec<2>(zv, sl);
+        if (sl[0] >= 0) fix.add(sl[0], t.c[PHK_X].x, t.c[PHK_Y].x);
+        if (sl[1] >= 0) fix.add(sl[1], t.c[PHK_X].y, t.c[PHK_Y].y);
+    }
+}
+
 template <int SHAPE, bool PK, bool ACC>
 __global__ void __launch_bounds__(kStreamThreads, 4)
 stream_kernel(const __grid_constant__ StreamProg sp,
@@ -245,6 +451,7 @@ stream_kernel(const __grid_constant__ StreamProg sp,
               const __grid_constant__ phk_accum acc,
               const __grid_constant__ StreamArgs a) {
     namespace cg = cooperative_groups;
+    using Acc = typename std::conditional<kStreamWords, FixWords, FixHist>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     const int Sa = ACC ? acc.slicer.n_slices : 0;
     const int Sp = PK ? pk.slicer.n_slices : 0;
@@ -252,6 +459,7 @@ stream_kernel(const __grid_constant__ StreamProg sp,
     stream_smem_layout(Sa, Sp, a.n_tables, a.stages, off);
     int* hcnt = reinterpret_cast<int*>(smem + off[0]);
     int* fdig = reinterpret_cast<int*>(smem + off[1]);
+    unsigned long long* fw = reinterpret_cast<unsigned long long*>(smem + off[0]);
     unsigned* fflag = reinterpret_cast<unsigned*>(smem + off[2]);
     float* eacc = reinterpret_cast<float*>(smem + off[3]);
     float* epk = reinterpret_cast<float*>(smem + off[4]);
@@ -267,42 +475,6 @@ stream_kernel(const __grid_constant__ StreamProg sp,
                   (size_t)warp * stages * 6 * kStreamTile;
     unsigned long long* wb =
         reinterpret_cast<unsigned long long*>(smem + off[7]) + warp * stages;
-    if (tid == 0) {
-        s_max[0] = s_max[1] = 0u;
-        s_abort = 0;
-        s_undrained = 0;
-    }
-    if (lane == 0) {
-        for (int st = 0; st < stages; ++st) mbar_init(wb + st, 1);
-        mbar_fence_init();
-    }
-    if constexpr (ACC) {
-        const float* e = reinterpret_cast<const float*>(acc.slicer.edges);
-        for (int i = tid; i <= Sa; i += kStreamThreads) eacc[i] = e[i];
-        for (int i = tid; i < Sa; i += kStreamThreads) hcnt[i] = 0;
-        for (int i = tid; i < 6 * Sa; i += kStreamThreads) fdig[i] = 0;
-        for (int i = tid; i < (Sa + 3) / 4; i += kStreamThreads) fflag[i] = 0u;
-    }
-    if constexpr (PK) {
-        TrackArgs ta;
-        ta.kick_comb = 1;
-        ta.kicks_smem = 1;
-        for (int q = 0; q < 3; ++q) ta.comb_slot[q] = a.comb_slot[q];
-        stage_pending<float>(pk, ta, epk, ktab, tid, kStreamThreads);
-    }
-    __syncthreads();
-    Bins<float> bpk, bac;
-    if constexpr (PK) bpk.init(epk, Sp, pk.slicer.negate);
-    if constexpr (ACC) bac.init(eacc, Sa, acc.slicer.negate);
-    vote_fast_path<float>(bpk, PK, tid, kStreamThreads);
-    vote_fast_path<float>(bac, ACC, tid, kStreamThreads);
-
-    const bool clustered = ACC && a.cluster > 1;
-    const unsigned crank = clustered ? cg::this_cluster().block_rank() : 0u;
-    const int column = clustered ? (int)(blockIdx.x / a.cluster) : (int)blockIdx.x;
-    const int G = acc.grid;
-    double* P = acc.partials;
-
     // warp-tiles: full ones through the ring, the partial last one (if
     // any) with plain loads by the warp that owns its index
     const int GW = (int)gridDim.x * kStreamWarps;
@@ -327,13 +499,55 @@ stream_kernel(const __grid_constant__ StreamProg sp,
                          a.c[q] + tile * kStreamTile, kStreamTile * 4, wb + st);
         last[st] = k;
     };
-    if (lane == 0)
+    if (tid == 0) {
+        s_max[0] = s_max[1] = 0u;
+        s_abort = 0;
+        s_undrained = 0;
+    }
+    if (lane == 0) {
+        for (int st = 0; st < stages; ++st) mbar_init(wb + st, 1);
+        mbar_fence_init();
+        // the warp's first tiles are on their way while the CTA stages its
+        // tables (each warp's ring has shared memory of its own)
         for (int k = 0; k < mine && k < stages; ++k) issue(k, k);
+    }
+    if constexpr (ACC) {
+        const float* e = reinterpret_cast<const float*>(acc.slicer.edges);
+        for (int i = tid; i <= Sa; i += kStreamThreads) eacc[i] = e[i];
+        if constexpr (kStreamWords) {
+            for (int i = tid; i < 2 * Sa; i += kStreamThreads) fw[i] = 0ull;
+        } else {
+            for (int i = tid; i < Sa; i += kStreamThreads) hcnt[i] = 0;
+            for (int i = tid; i < 4 * Sa; i += kStreamThreads) fdig[i] = 0;
+        }
+        for (int i = tid; i < (Sa + 3) / 4; i += kStreamThreads) fflag[i] = 0u;
+    }
+    if constexpr (PK) {
+        TrackArgs ta;
+        ta.kick_comb = 1;
+        ta.kicks_smem = 1;
+        for (int q = 0; q < 3; ++q) ta.comb_slot[q] = a.comb_slot[q];
+        stage_pending<float>(pk, ta, epk, ktab, tid, kStreamThreads);
+    }
+    __syncthreads();
+    Bins<float> bpk, bac;
+    if constexpr (PK) bpk.init(epk, Sp, pk.slicer.negate);
+    if constexpr (ACC) bac.init(eacc, Sa, acc.slicer.negate);
+    vote_fast_path<float>(bpk, PK, tid, kStreamThreads);
+    vote_fast_path<float>(bac, ACC, tid, kStreamThreads);
+
+    const bool clustered = ACC && a.cluster > 1;
+    const unsigned crank = clustered ? cg::this_cluster().block_rank() : 0u;
+    const int column = clustered ? (int)(blockIdx.x / a.cluster) : (int)blockIdx.x;
+    const int G = acc.grid;
+    double* P = acc.partials;
+    long long* PL = reinterpret_cast<long long*>(P);
+
     bool bad = false;
 
-    FixHist fix;
+    Acc fix;
     if constexpr (ACC) {
-        // ---- the cluster's FixHist scale, from each warp's first tile
+        // ---- the cluster's fixed-point scale, from each warp's first tile
         unsigned m[2] = {0u, 0u};
         auto see = [&](float u, int q) {
             const unsigned b = __float_as_uint(u) & 0x7fffffffu;
@@ -364,14 +578,17 @@ stream_kernel(const __grid_constant__ StreamProg sp,
             atomicMax(&s_max[1], m[1]);
         }
         if (tid == 0) {
-            s_spill.spill[0] = reinterpret_cast<long long*>(P) + (int64_t)Sa * G + column;
-            s_spill.spill[1] = reinterpret_cast<long long*>(P) + (int64_t)2 * Sa * G + column;
+            s_spill.spill[0] = PL + (int64_t)Sa * G + column;
+            s_spill.spill[1] = PL + (int64_t)2 * Sa * G + column;
             s_spill.stride = G;
         }
         if (crank == 0) {
+            // level-B sums (and, with FixWords, flushed counts) of the
+            // column start at zero
             for (int s = tid; s < Sa; s += kStreamThreads) {
-                reinterpret_cast<long long*>(P)[(int64_t)(Sa + s) * G + column] = 0;
-                reinterpret_cast<long long*>(P)[(int64_t)(2 * Sa + s) * G + column] = 0;
+                if (kStreamWords) PL[(int64_t)s * G + column] = 0;
+                PL[(int64_t)(Sa + s) * G + column] = 0;
+                PL[(int64_t)(2 * Sa + s) * G + column] = 0;
             }
         }
         unsigned M[2];
@@ -390,8 +607,7 @@ stream_kernel(const __grid_constant__ StreamProg sp,
             M[0] = s_max[0];
             M[1] = s_max[1];
         }
-        fix.cnt = hcnt;
-        fix.dig = fdig;
+        acc_bind(fix, fw, hcnt, fdig);
         fix.flag = fflag;
         fix.sp = &s_spill;
         fix.S = Sa;
@@ -400,9 +616,14 @@ stream_kernel(const __grid_constant__ StreamProg sp,
     }
 
     // ---- the warp's full tiles.  The loop runs the CTA's count so that
-    // every warp reaches the FixHist flush barriers; a warp past its own
-    // tiles, or after a wait gave up anywhere in the CTA, only keeps pace.
-    constexpr int kStore = stream_store_bits<SHAPE>();
+    // every warp reaches the flush barriers of the slice sums; a warp past
+    // its own tiles, or after a wait gave up anywhere in the CTA, only keeps
+    // pace.
+    constexpr int kStore = stream_store_bits<SHAPE>() | (PK ? 0x0A : 0);
+    constexpr int kLoad = stream_load_bits<SHAPE, PK, ACC>();
+    constexpr int kFlushEvery =
+        (int)((kStreamWords ? kFix64MaxPerCta : kFixMaxPerCta) /
+              (kStreamWarps * kStreamTile));
     volatile int* abort_flag = &s_abort;
     int st = 0;
     unsigned ph = 0u;
@@ -417,39 +638,31 @@ stream_kernel(const __grid_constant__ StreamProg sp,
         }
         if (ok) {
             const float* src = ring + (size_t)st * 6 * kStreamTile + lane * 2;
-            constexpr int kLoad = stream_load_bits<SHAPE, PK, ACC>();
-            float2 v[6];
+            Pair t;
 #pragma unroll
             for (int q = 0; q < 6; ++q)
-                v[q] = ((kLoad >> q) & 1)
-                           ? *reinterpret_cast<const float2*>(src + q * kStreamTile)
-                           : make_float2(0.f, 0.f);
-            Tile<float, 1> t0, t1;
-#pragma unroll
-            for (int q = 0; q < 6; ++q) { t0.c[q][0] = v[q].x; t1.c[q][0] = v[q].y; }
-            stream_particle<SHAPE, PK, ACC>(sp, a, bpk, bac, ktab, Sp, fix, t0);
-            stream_particle<SHAPE, PK, ACC>(sp, a, bpk, bac, ktab, Sp, fix, t1);
+                t.c[q] = ((kLoad >> q) & 1)
+                             ? *reinterpret_cast<const float2*>(src + q * kStreamTile)
+                             : make_float2(0.f, 0.f);
+            __syncwarp();                   // the warp's reads of stage st done
+            if (lane == 0 && k + stages < mine && !*abort_flag) issue(k + stages, st);
+            stream_pair<SHAPE, PK, ACC>(sp, a, bpk, bac, ktab, Sp, fix, t);
             const int off = (gw + k * GW) * kStreamTile + lane * 2;
 #pragma unroll
             for (int q = 0; q < 6; ++q) {
-                constexpr int kSt = kStore | (PK ? 0x0A : 0);
-                const bool w = ((kSt >> q) & 1) ||
+                const bool w = ((kStore >> q) & 1) ||
                                (PK && q == PHK_DP && a.comb_slot[2] >= 0);
-                if (w) __stcs(reinterpret_cast<float2*>(a.c[q] + off),
-                              make_float2(t0.c[q][0], t1.c[q][0]));
+                if (w) __stcs(reinterpret_cast<float2*>(a.c[q] + off), t.c[q]);
             }
         }
-        __syncwarp();                       // the warp's reads of stage st done
-        if (lane == 0 && ok && k + stages < mine && !*abort_flag)
-            issue(k + stages, st);
         if (++st == stages) {
             st = 0;
             ph ^= 1u;
         }
         if constexpr (ACC) {
-            if ((k + 1) % (int)(kFixMaxPerCta / (kStreamWarps * kStreamTile)) == 0) {
+            if ((k + 1) % kFlushEvery == 0) {
                 __syncthreads();
-                fix_flush(fix, tid, kStreamThreads);
+                acc_flush(fix, PL + column, tid, kStreamThreads);
                 __syncthreads();
             }
         }
@@ -463,14 +676,12 @@ stream_kernel(const __grid_constant__ StreamProg sp,
             const bool live = i0 + j < a.n;
 #pragma unroll
             for (int q = 0; q < 6; ++q)
-                t[j].c[q][0] = (live && ((stream_load_bits<SHAPE, PK, ACC>() >> q) & 1))
-                                   ? a.c[q][i0 + j] : 0.f;
+                t[j].c[q][0] = (live && ((kLoad >> q) & 1)) ? a.c[q][i0 + j] : 0.f;
             if (!live) continue;
             stream_particle<SHAPE, PK, ACC>(sp, a, bpk, bac, ktab, Sp, fix, t[j]);
 #pragma unroll
             for (int q = 0; q < 6; ++q) {
-                constexpr int kSt = kStore | (PK ? 0x0A : 0);
-                const bool w = ((kSt >> q) & 1) ||
+                const bool w = ((kStore >> q) & 1) ||
                                (PK && q == PHK_DP && a.comb_slot[2] >= 0);
                 if (w) a.c[q][i0 + j] = t[j].c[q][0];
             }
@@ -500,29 +711,36 @@ stream_kernel(const __grid_constant__ StreamProg sp,
             nb = cl.num_blocks();
         }
         if (crank == 0) {
-            const long long* lp = reinterpret_cast<const long long*>(P);
             for (int s = tid; s < Sa; s += kStreamThreads) {
-                long long c = 0, tq[2];
+                long long c = kStreamWords ? __ldcg(PL + (int64_t)s * G + column) : 0;
+                long long tq[2];
                 unsigned fl = 0;
-                tq[0] = __ldcg(lp + (int64_t)(Sa + s) * G + column);
-                tq[1] = __ldcg(lp + (int64_t)(2 * Sa + s) * G + column);
+                tq[0] = __ldcg(PL + (int64_t)(Sa + s) * G + column);
+                tq[1] = __ldcg(PL + (int64_t)(2 * Sa + s) * G + column);
                 for (unsigned r = 0; r < nb; ++r) {
-                    const int* rc = hcnt;
-                    const int* rd = fdig;
                     const unsigned* rf = fflag;
-                    if (clustered) {
-                        cg::cluster_group cl = cg::this_cluster();
-                        rc = cl.map_shared_rank(hcnt, r);
-                        rd = cl.map_shared_rank(fdig, r);
-                        rf = cl.map_shared_rank(fflag, r);
-                    }
-                    c += rc[s];
+                    if (clustered) rf = cg::this_cluster().map_shared_rank(fflag, r);
                     fl |= (rf[s >> 2] >> (8 * (s & 3))) & 0xffu;
+                    if constexpr (kStreamWords) {
+                        const unsigned long long* rw = fw;
+                        if (clustered) rw = cg::this_cluster().map_shared_rank(fw, r);
+                        long long n, sx;
+                        FixWords::split(rw[s], &n, &sx);
+                        c += n;
+                        tq[0] += sx;
+                        tq[1] += (long long)rw[Sa + s];
+                    } else {
+                        const int* rc = hcnt;
+                        const int* rd = fdig;
+                        if (clustered) {
+                            cg::cluster_group cl = cg::this_cluster();
+                            rc = cl.map_shared_rank(hcnt, r);
+                            rd = cl.map_shared_rank(fdig, r);
+                        }
+                        c += rc[s];
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        const int* d = rd + 3 * q * Sa + s;
-                        tq[q] += (long long)d[0] + ((long long)d[Sa] << 11) +
-                                 ((long long)d[2 * Sa] << 21);
+                        for (int q = 0; q < 2; ++q)
+                            tq[q] += FixHist::total(rd + 2 * q * Sa + s, Sa);
                     }
                 }
                 P[(int64_t)s * G + column] = (double)c;

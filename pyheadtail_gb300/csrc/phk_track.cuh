@@ -882,11 +882,12 @@ __device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
 // cluster's first tiles so that it maps to [2^26, 2^27).  A value u becomes
 // the integer v = rint(u 2^k) (u 2^k is exact; the rounding is the only
 // approximation, at most 2^-28 of that largest value, below the FP32
-// rounding of u itself).  Level A, |u 2^k| < 2^30: v is split into three
-// digits d0 = v & 0x7ff, d1 = (v >> 11) & 0x3ff, d2 = v >> 21 (arithmetic)
-// that are added to 32-bit counters with shared-memory atomics; each digit
-// is below 2^11 in magnitude, so 2^20 values per counter cannot overflow
-// (a CTA adds its counters to level B every 2^20 values).  Level B, larger
+// rounding of u itself).  Level A, |u 2^k| < 2^30: v is split into two
+// 15-bit digits d0 = v & 0x7fff in [0, 2^15) and d1 = v >> 15 (arithmetic)
+// in [-2^15, 2^15), added to 32-bit counters with shared-memory atomics
+// (two per coordinate, one for the count: five per particle); 2^16 values
+// per counter stay inside the int32 range (a CTA adds its counters to level
+// B at least every 2^16 values).  Level B, larger
 // finite values (2^30 <= |u 2^k| < 2^40, rare): 64-bit atomics at the same
 // scale on the cluster's partial column in global memory, zeroed by the
 // cluster's rank 0 before the first add.  Level C: NaN, +-inf and
@@ -899,7 +900,7 @@ __device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
 // -------------------------------------------------------------------
 constexpr float kFixLevelA = 1073741824.0f;        // 2^30
 constexpr float kFixLevelB = 1099511627776.0f;     // 2^40
-constexpr int64_t kFixMaxPerCta = (int64_t)1 << 20;  // values per counter
+constexpr int64_t kFixMaxPerCta = (int64_t)1 << 16;  // values per counter
 
 // Levels B and C of one value (rare; kept out of line): v = u 2^k.
 static __device__ __noinline__ void fix_add_slow(long long* spill,
@@ -924,7 +925,7 @@ struct FixSpill {
 
 struct FixHist {
     int* cnt;             // [S] counts
-    int* dig;             // [6][S]: x d0 d1 d2, y d0 d1 d2
+    int* dig;             // [4][S]: x d0 d1, y d0 d1
     unsigned* flag;       // [(S + 3) / 4]: one byte per slice, x low nibble
     const FixSpill* sp;   // in shared memory
     int S;
@@ -934,10 +935,9 @@ struct FixHist {
         const float v = u * scale[q];
         if (fabsf(v) < kFixLevelA) {
             const int iv = __float2int_rn(v);
-            int* d = dig + 3 * q * S + s;
-            atomicAdd(d, iv & 0x7ff);
-            atomicAdd(d + S, (iv >> 11) & 0x3ff);
-            atomicAdd(d + 2 * S, iv >> 21);
+            int* d = dig + 2 * q * S + s;
+            atomicAdd(d, iv & 0x7fff);
+            atomicAdd(d + S, iv >> 15);
         } else {
             fix_add_slow(sp->spill[q] + (int64_t)s * sp->stride,
                          flag + (s >> 2), 8 * (s & 3) + 4 * q, u, v);
@@ -948,7 +948,89 @@ struct FixHist {
         add_q(0, s, x);
         add_q(1, s, y);
     }
+    // the sum held by the two digit counters at d and d + S
+    static __device__ __forceinline__ long long total(const int* d, int S) {
+        return (long long)d[0] + ((long long)d[S] << 15);
+    }
 };
+
+// -------------------------------------------------------------------
+// FixWords: the same exact sums as FixHist in two 64-bit words per slice,
+// updated with one 64-bit shared-memory atomic each.  Word 0 carries the
+// count in its top bits: every particle adds 2^44 + v_x, so after n adds
+// word 0 = n 2^44 + sum v_x; with |v| < 2^27 and at most 2^15 values per
+// word between flushes, |sum v_x| < 2^42, and n = (w0 + 2^43) >> 44,
+// sum v_x = w0 - n 2^44 recover both.  Word 1 is sum v_y.  Values with
+// |v| >= 2^27 (or non-finite) take the level B / C paths of FixHist, their
+// count still going into word 0.  A CTA flushes its words into the level-B
+// columns (counts into the count column) every 2^15 values.  The totals are
+// the exact integer sums of rint(u 2^k), identical to FixHist's.
+// -------------------------------------------------------------------
+constexpr float kFix64A = 134217728.0f;                 // 2^27
+constexpr long long kFix64Count = (long long)1 << 44;
+constexpr int64_t kFix64MaxPerCta = (int64_t)1 << 15;   // values per word
+
+struct FixWords {
+    unsigned long long* w;   // [2][S]: count + sum x, sum y
+    unsigned* flag;          // [(S + 3) / 4]
+    const FixSpill* sp;      // level-B columns (shared memory)
+    int S;
+    float scale[2];
+
+    static __device__ __noinline__ void add_slow(const FixWords& f, int s,
+                                                 float x, float y, float vx,
+                                                 float vy) {
+        const bool ax = fabsf(vx) < kFix64A, ay = fabsf(vy) < kFix64A;
+        atomicAdd(f.w + s, (unsigned long long)(kFix64Count +
+                                                (ax ? (long long)__float2int_rn(vx) : 0)));
+        if (ay) atomicAdd(f.w + f.S + s, (unsigned long long)(long long)__float2int_rn(vy));
+        if (!ax)
+            fix_add_slow(f.sp->spill[0] + (int64_t)s * f.sp->stride,
+                         f.flag + (s >> 2), 8 * (s & 3), x, vx);
+        if (!ay)
+            fix_add_slow(f.sp->spill[1] + (int64_t)s * f.sp->stride,
+                         f.flag + (s >> 2), 8 * (s & 3) + 4, y, vy);
+    }
+    __device__ __forceinline__ void add(int s, float x, float y) const {
+        const float vx = x * scale[0], vy = y * scale[1];
+        if (fabsf(vx) < kFix64A && fabsf(vy) < kFix64A) {
+            atomicAdd(w + s, (unsigned long long)(kFix64Count +
+                                                  (long long)__float2int_rn(vx)));
+            atomicAdd(w + S + s, (unsigned long long)(long long)__float2int_rn(vy));
+        } else {
+            add_slow(*this, s, x, y, vx, vy);
+        }
+    }
+    // count and sum v_x of a word 0
+    static __device__ __forceinline__ void split(unsigned long long w0,
+                                                 long long* n, long long* sx) {
+        const long long v = (long long)w0;
+        *n = (v + ((long long)1 << 43)) >> 44;
+        *sx = v - (*n << 44);
+    }
+};
+
+// Adds the FixWords of this CTA to the level-B columns (counts to the
+// count column `cnt`, stride as the sums) and clears them (all threads,
+// between two barriers).
+__device__ __forceinline__ void fix_words_flush(const FixWords& f,
+                                                long long* cnt, int tid,
+                                                int nthreads) {
+    for (int s = tid; s < f.S; s += nthreads) {
+        long long n, sx;
+        FixWords::split(f.w[s], &n, &sx);
+        const long long sy = (long long)f.w[f.S + s];
+        const int64_t o = (int64_t)s * f.sp->stride;
+        if (n) atomicAdd(reinterpret_cast<unsigned long long*>(cnt + o),
+                         (unsigned long long)n);
+        if (sx) atomicAdd(reinterpret_cast<unsigned long long*>(f.sp->spill[0] + o),
+                          (unsigned long long)sx);
+        if (sy) atomicAdd(reinterpret_cast<unsigned long long*>(f.sp->spill[1] + o),
+                          (unsigned long long)sy);
+        f.w[s] = 0ull;
+        f.w[f.S + s] = 0ull;
+    }
+}
 
 // 2^k, the FixHist scale for the largest finite magnitude m (as float bits;
 // 0 when there is none): m 2^k in [2^26, 2^27)
@@ -1052,7 +1134,7 @@ __device__ __forceinline__ float tmul<float>(float a, float b) { return a * b; }
 //   histogram: bid-serialised words [3][n_hist][Sa] (sum x, sum y as
 //              Hist<T>::Word; count as int in the third region), or with
 //              `fix` (FP32 single bunch) the FixHist counters: count [Sa],
-//              digits [6][Sa], flag bytes [Sa] (ints)
+//              digits [4][Sa], flag bytes [Sa] (ints)
 //   accumulation edges [Sa + 1] T, pending-kick edges [Sp + 1] T,
 //   kick tables [n_tables][Sp] T (when staged), bid tags [n_hist][Sa] int
 //   (none with `fix`), TMA ring [stages][6][tile] T, one mbarrier per stage
@@ -1066,7 +1148,7 @@ __host__ __device__ inline size_t track_smem_layout(int Sa, int Sp, int n_hist,
     size_t b = 0;
     if (fix) {
         off[0] = b; b = align16(b + (size_t)4 * Sa);              // count
-        off[1] = b; b = align16(b + (size_t)4 * 6 * Sa);          // digits
+        off[1] = b; b = align16(b + (size_t)4 * 4 * Sa);          // digits
         off[2] = b; b = align16(b + (size_t)4 * ((Sa + 3) / 4));  // flags
     } else {
         off[0] = b; b = align16(b + (size_t)8 * n_hist * Sa);   // sum x words
@@ -1415,7 +1497,7 @@ __device__ __forceinline__ void load_tile_plain(const TrackArgs& a,
 // is compiled for (register cap) and the shared memory a CTA may plan for
 constexpr int kF32Vec = 2;
 constexpr int kF32MinBlocks = 4;
-constexpr size_t kF32SmemBudget = 54 * 1024;
+constexpr size_t kF32SmemBudget = 56 * 1024;
 constexpr size_t kF64SmemBudget = 112 * 1024;
 
 // polls of one mbarrier phase before a kernel gives up (order of a second)
@@ -1435,14 +1517,13 @@ __device__ __forceinline__ void fix_flush(const FixHist& f, int tid,
     for (int s = tid; s < f.S; s += nthreads) {
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-            int* d = f.dig + 3 * q * f.S + s;
-            const long long t = (long long)d[0] + ((long long)d[f.S] << 11) +
-                                ((long long)d[2 * f.S] << 21);
+            int* d = f.dig + 2 * q * f.S + s;
+            const long long t = FixHist::total(d, f.S);
             if (t != 0)
                 atomicAdd(reinterpret_cast<unsigned long long*>(
                               f.sp->spill[q] + (int64_t)s * f.sp->stride),
                           (unsigned long long)t);
-            d[0] = 0; d[f.S] = 0; d[2 * f.S] = 0;
+            d[0] = 0; d[f.S] = 0;
         }
     }
 }
@@ -1485,19 +1566,45 @@ track_kernel(const __grid_constant__ phk_program prog,
     __shared__ int s_rel[kMaxStages], s_last[kMaxStages], s_abort;
 
     const int tid = threadIdx.x;
+    const int64_t full_tiles = a.n / TILE;
+    const int64_t mine = (a.stages > 0 && blockIdx.x < full_tiles)
+                             ? (full_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x
+                             : 0;
+    const bool has_partial = a.stages > 0 && a.n % TILE != 0 &&
+                             blockIdx.x == (int)(full_tiles % gridDim.x);
+    int nq = 0;
+    for (int q = 0; q < 6; ++q) nq += (a.load_mask >> q) & 1;
+    const unsigned stage_bytes = (unsigned)(nq * TILE * sizeof(T));
+    // bulk copies of this CTA's k-th tile into stage st (one thread)
+    auto issue = [&](int64_t k, int st) {
+        const int64_t tile = blockIdx.x + k * gridDim.x;
+        fence_proxy_async_smem();
+        mbar_expect_tx(bars + st, stage_bytes);
+        for (int q = 0; q < 6; ++q)
+            if ((a.load_mask >> q) & 1)
+                bulk_g2s(ring + ((size_t)st * 6 + q) * TILE,
+                         reinterpret_cast<T*>(a.c[q]) + tile * TILE,
+                         TILE * sizeof(T), bars + st);
+        s_last[st] = (int)k;
+    };
     if (tid == 0) {
         s_max[0] = s_max[1] = 0u;
         s_abort = 0;
         for (int st = 0; st < kMaxStages; ++st) s_rel[st] = 0, s_last[st] = -1;
         for (int st = 0; st < a.stages; ++st) mbar_init(bars + st, 1);
-        if (a.stages > 0) mbar_fence_init();
+        if (a.stages > 0) {
+            mbar_fence_init();
+            // the first tiles are on their way while the CTA stages its
+            // tables (the ring has shared memory of its own)
+            for (int64_t k = 0; k < mine && k < a.stages; ++k) issue(k, (int)k);
+        }
     }
     if (a.has_acc) {
         const T* e = reinterpret_cast<const T*>(acc.slicer.edges);
         for (int i = tid; i <= Sa; i += blockDim.x) stage_edge<T>(eacc, i, e[i]);
         if constexpr (FIX) {
             for (int i = tid; i < Sa; i += blockDim.x) hcnt[i] = 0;
-            for (int i = tid; i < 6 * Sa; i += blockDim.x) fdig[i] = 0;
+            for (int i = tid; i < 4 * Sa; i += blockDim.x) fdig[i] = 0;
             for (int i = tid; i < (Sa + 3) / 4; i += blockDim.x) fflag[i] = 0u;
         } else {
             for (int i = tid; i < a.n_hist * Sa; i += blockDim.x) {
@@ -1532,28 +1639,6 @@ track_kernel(const __grid_constant__ phk_program prog,
     const int G = acc.grid;
     double* P = acc.partials;
 
-    const int64_t full_tiles = a.n / TILE;
-    const int64_t mine = (a.stages > 0 && blockIdx.x < full_tiles)
-                             ? (full_tiles - blockIdx.x + gridDim.x - 1) / gridDim.x
-                             : 0;
-    const bool has_partial = a.stages > 0 && a.n % TILE != 0 &&
-                             blockIdx.x == (int)(full_tiles % gridDim.x);
-    int nq = 0;
-    for (int q = 0; q < 6; ++q) nq += (a.load_mask >> q) & 1;
-    const unsigned stage_bytes = (unsigned)(nq * TILE * sizeof(T));
-    // bulk copies of this CTA's k-th tile into stage st (one thread)
-    auto issue = [&](int64_t k, int st) {
-        const int64_t tile = blockIdx.x + k * gridDim.x;
-        fence_proxy_async_smem();
-        mbar_expect_tx(bars + st, stage_bytes);
-        for (int q = 0; q < 6; ++q)
-            if ((a.load_mask >> q) & 1)
-                bulk_g2s(ring + ((size_t)st * 6 + q) * TILE,
-                         cx.cp[q] + tile * TILE, TILE * sizeof(T), bars + st);
-        s_last[st] = (int)k;
-    };
-    if (a.stages > 0 && tid == 0)
-        for (int64_t k = 0; k < mine && k < a.stages; ++k) issue(k, (int)k);
     bool bad = false;   // a bounded copy wait of this thread gave up
 
     if constexpr (FIX) {
@@ -1771,11 +1856,8 @@ track_kernel(const __grid_constant__ phk_program prog,
                     c += rc[s];
                     fl |= (rf[s >> 2] >> (8 * (s & 3))) & 0xffu;
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        const int* d = rd + 3 * q * Sa + s;
-                        tq[q] += (long long)d[0] + ((long long)d[Sa] << 11) +
-                                 ((long long)d[2 * Sa] << 21);
-                    }
+                    for (int q = 0; q < 2; ++q)
+                        tq[q] += FixHist::total(rd + 2 * q * Sa + s, Sa);
                 }
                 P[(int64_t)s * G + column] = (double)c;
                 P[(int64_t)(Sa + s) * G + column] =

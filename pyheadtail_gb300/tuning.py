@@ -28,8 +28,8 @@ DEFAULT_PLAN = (-1, -1, -1)
 # (variant, stages, shared-memory KB): the tile-shared kernel (0) with the
 # TMA ring of 0 / 2 / 3 stages at four, three or two CTAs per SM, and the
 # streaming kernel (1) with 2-4 stages per warp
-CANDIDATES = ([(0, s, kb) for s in (0, 2, 3) for kb in (54, 72, 108)] +
-              [(1, s, kb) for s in (2, 3, 4) for kb in (54, 72, 108)])
+CANDIDATES = ([(0, s, kb) for s in (0, 2, 3) for kb in (56, 72, 108)] +
+              [(1, s, kb) for s in (2, 3, 4) for kb in (56, 72, 108)])
 
 _state = {'enabled': False, 'cache_path': None, 'cache': None,
           'tuned': {}}
@@ -101,11 +101,19 @@ def plan_for(engine, prog, coords, ks, ac, ops, kick, acc, stream):
         return plan
     if torch.cuda.is_current_stream_capturing():
         return DEFAULT_PLAN
-    plan, ms = _time_candidates(engine, prog, coords, ks, ac, stream)
-    cache[key] = {'plan': list(plan), 'ms': ms}
+    plan, ms, every = _time_candidates(engine, prog, coords, ks, ac, stream)
+    cache[key] = {'plan': list(plan), 'ms': ms,
+                  'candidates': {'%d,%d,%d' % c: t for c, t in every.items()}}
     _state['tuned'][key] = plan
     _store()
     return plan
+
+
+def _last_variant():
+    v, s, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    N.call('phk_last_track_launch', ctypes.byref(v), ctypes.byref(s),
+           ctypes.byref(m))
+    return v.value
 
 
 def _time_candidates(engine, prog, coords, ks, ac, stream, reps=3):
@@ -133,9 +141,18 @@ def _time_candidates(engine, prog, coords, ks, ac, stream, reps=3):
                 torch.cuda.synchronize()
                 if it:
                     times.append(e0.elapsed_time(e1))
-            results[cand] = float(np.median(times))
+            # a plan whose shared memory does not fit runs the other kernel:
+            # only plans that launched as asked compete
+            if _last_variant() == cand[0]:
+                results[cand] = float(np.median(times))
     finally:
         N.call('phk_set_track_plan', *DEFAULT_PLAN)
     del scratch
     best = min(results, key=results.get)
-    return best, results[best]
+    return best, results[best], results
+
+
+def timings():
+    """Every tuned configuration of the cache: {key: {'plan', 'ms',
+    'candidates': {'variant,stages,kb': ms}}}."""
+    return dict(_load()) if _state['cache_path'] else {}
