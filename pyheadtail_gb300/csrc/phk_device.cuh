@@ -69,6 +69,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar,
     return false;
 }
 
+
 // ---------------------------------------------------------------- helpers
 // The plain form reproduces the reference's NumPy evaluation order, so each
 // product and sum is rounded on its own (no FMA contraction).

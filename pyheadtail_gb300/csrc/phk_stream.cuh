@@ -21,11 +21,7 @@ constexpr int kStreamThreads = kStreamWarps * 32;
 constexpr int kStreamTile = 64;          // particles per warp-tile
 constexpr int kStreamMaxStages = 4;
 constexpr size_t kStreamSmemBudget = 56 * 1024;
-#ifndef PHK_STREAM_WORDS
-#define PHK_STREAM_WORDS 0
-#endif
-// slice sums of the streaming kernel: FixWords (1) or FixHist (0)
-constexpr bool kStreamWords = PHK_STREAM_WORDS != 0;
+
 
 struct StreamArgs {
     float* c[6];
@@ -346,13 +342,8 @@ __host__ __device__ inline size_t stream_smem_layout(int Sa, int Sp,
                                                      int n_tables, int stages,
                                                      size_t* off) {
     size_t b = 0;
-    if (kStreamWords) {
-        off[0] = b; b = align16(b + (size_t)8 * 2 * Sa);     // FixWords
-        off[1] = b;
-    } else {
-        off[0] = b; b = align16(b + (size_t)4 * Sa);          // FixHist count
-        off[1] = b; b = align16(b + (size_t)4 * 4 * Sa);      // digits
-    }
+    off[0] = b; b = align16(b + (size_t)4 * Sa);              // FixHist count
+    off[1] = b; b = align16(b + (size_t)4 * 4 * Sa);          // digits
     off[2] = b; b = align16(b + (size_t)4 * ((Sa + 3) / 4));
     off[3] = b; b = align16(b + (size_t)4 * (Sa > 0 ? Sa + 1 : 0));
     off[4] = b; b = align16(b + (size_t)4 * (Sp > 0 ? Sp + 1 : 0));
@@ -369,13 +360,13 @@ constexpr int stream_store_bits() {
 }
 
 // pending kicks, program, accumulation of one particle
-template <int SHAPE, bool PK, bool ACC, typename F>
+template <int SHAPE, bool PK, bool ACC>
 __device__ __forceinline__ void stream_particle(const StreamProg& sp,
                                                 const StreamArgs& a,
                                                 const Bins<float>& bpk,
                                                 const Bins<float>& bac,
                                                 const float* ktab, int Sp,
-                                                const F& fix,
+                                                const FixHist& fix,
                                                 Tile<float, 1>& t) {
     if constexpr (PK) {
         const int s = bpk.index(t.c[PHK_Z][0]);
@@ -392,33 +383,14 @@ __device__ __forceinline__ void stream_particle(const StreamProg& sp,
     }
 }
 
-// the slice-sum accumulator's shared arrays and its periodic flush
-__device__ __forceinline__ void acc_bind(FixWords& f, unsigned long long* fw,
-                                         int*, int*) {
-    f.w = fw;
-}
-__device__ __forceinline__ void acc_bind(FixHist& f, unsigned long long*,
-                                         int* cnt, int* dig) {
-    f.cnt = cnt;
-    f.dig = dig;
-}
-__device__ __forceinline__ void acc_flush(const FixWords& f, long long* cnt,
-                                          int tid, int nthreads) {
-    fix_words_flush(f, cnt, tid, nthreads);
-}
-__device__ __forceinline__ void acc_flush(const FixHist& f, long long*,
-                                          int tid, int nthreads) {
-    fix_flush(f, tid, nthreads);
-}
-
 // pending kicks, program and accumulation of the lane's two particles
-template <int SHAPE, bool PK, bool ACC, typename F>
+template <int SHAPE, bool PK, bool ACC>
 __device__ __forceinline__ void stream_pair(const StreamProg& sp,
                                             const StreamArgs& a,
                                             const Bins<float>& bpk,
                                             const Bins<float>& bac,
                                             const float* ktab, int Sp,
-                                            const F& fix, Pair& t) {
+                                            const FixHist& fix, Pair& t) {
     if constexpr (PK) {
         const float zv[2] = {t.c[PHK_Z].x, t.c[PHK_Z].y};
         int sl[2];
@@ -451,7 +423,6 @@ stream_kernel(const __grid_constant__ StreamProg sp,
               const __grid_constant__ phk_accum acc,
               const __grid_constant__ StreamArgs a) {
     namespace cg = cooperative_groups;
-    using Acc = typename std::conditional<kStreamWords, FixWords, FixHist>::type;
     extern __shared__ __align__(16) unsigned char smem[];
     const int Sa = ACC ? acc.slicer.n_slices : 0;
     const int Sp = PK ? pk.slicer.n_slices : 0;
@@ -459,7 +430,6 @@ stream_kernel(const __grid_constant__ StreamProg sp,
     stream_smem_layout(Sa, Sp, a.n_tables, a.stages, off);
     int* hcnt = reinterpret_cast<int*>(smem + off[0]);
     int* fdig = reinterpret_cast<int*>(smem + off[1]);
-    unsigned long long* fw = reinterpret_cast<unsigned long long*>(smem + off[0]);
     unsigned* fflag = reinterpret_cast<unsigned*>(smem + off[2]);
     float* eacc = reinterpret_cast<float*>(smem + off[3]);
     float* epk = reinterpret_cast<float*>(smem + off[4]);
@@ -514,12 +484,8 @@ stream_kernel(const __grid_constant__ StreamProg sp,
     if constexpr (ACC) {
         const float* e = reinterpret_cast<const float*>(acc.slicer.edges);
         for (int i = tid; i <= Sa; i += kStreamThreads) eacc[i] = e[i];
-        if constexpr (kStreamWords) {
-            for (int i = tid; i < 2 * Sa; i += kStreamThreads) fw[i] = 0ull;
-        } else {
-            for (int i = tid; i < Sa; i += kStreamThreads) hcnt[i] = 0;
-            for (int i = tid; i < 4 * Sa; i += kStreamThreads) fdig[i] = 0;
-        }
+        for (int i = tid; i < Sa; i += kStreamThreads) hcnt[i] = 0;
+        for (int i = tid; i < 4 * Sa; i += kStreamThreads) fdig[i] = 0;
         for (int i = tid; i < (Sa + 3) / 4; i += kStreamThreads) fflag[i] = 0u;
     }
     if constexpr (PK) {
@@ -545,74 +511,35 @@ stream_kernel(const __grid_constant__ StreamProg sp,
 
     bool bad = false;
 
-    Acc fix;
+    FixHist fix;
     if constexpr (ACC) {
-        // ---- the cluster's fixed-point scale, from each warp's first tile
-        unsigned m[2] = {0u, 0u};
-        auto see = [&](float u, int q) {
-            const unsigned b = __float_as_uint(u) & 0x7fffffffu;
-            if (b < 0x7f800000u && b > m[q]) m[q] = b;
-        };
-        if (mine > 0) {
-            bad = !mbar_wait(wb, 0u, a.wait_limit);
-            if (!bad) {
-                const float* src = ring + lane * 2;
-                see(src[PHK_X * kStreamTile], 0);
-                see(src[PHK_X * kStreamTile + 1], 0);
-                see(src[PHK_Y * kStreamTile], 1);
-                see(src[PHK_Y * kStreamTile + 1], 1);
-            }
-        } else if (has_partial) {
-            const int64_t i0 = (int64_t)n_full * kStreamTile + lane * 2;
-            for (int j = 0; j < 2; ++j) {
-                if (i0 + j < a.n) {
-                    see(a.c[PHK_X][i0 + j], 0);
-                    see(a.c[PHK_Y][i0 + j], 1);
-                }
-            }
-        }
-        m[0] = __reduce_max_sync(0xffffffffu, m[0]);
-        m[1] = __reduce_max_sync(0xffffffffu, m[1]);
-        if (lane == 0) {
-            atomicMax(&s_max[0], m[0]);
-            atomicMax(&s_max[1], m[1]);
-        }
+        // ---- the fixed-point scales (the same in every CTA of every
+        // launch shape), then rank 0 clears its column's level-B sums
+        // before any member of the cluster adds to them
+        fix_sample_scales(a.c[PHK_X], a.c[PHK_Y], a.n, s_max, tid,
+                          kStreamThreads, fix.scale);
         if (tid == 0) {
             s_spill.spill[0] = PL + (int64_t)Sa * G + column;
             s_spill.spill[1] = PL + (int64_t)2 * Sa * G + column;
             s_spill.stride = G;
         }
         if (crank == 0) {
-            // level-B sums (and, with FixWords, flushed counts) of the
-            // column start at zero
             for (int s = tid; s < Sa; s += kStreamThreads) {
-                if (kStreamWords) PL[(int64_t)s * G + column] = 0;
                 PL[(int64_t)(Sa + s) * G + column] = 0;
                 PL[(int64_t)(2 * Sa + s) * G + column] = 0;
             }
         }
-        unsigned M[2];
         if (clustered) {
             __threadfence();
-            cg::cluster_group cl = cg::this_cluster();
-            cl.sync();
-            M[0] = M[1] = 0u;
-            for (unsigned r = 0; r < cl.num_blocks(); ++r) {
-                const unsigned* sm = cl.map_shared_rank(s_max, r);
-                M[0] = max(M[0], sm[0]);
-                M[1] = max(M[1], sm[1]);
-            }
+            cg::this_cluster().sync();
         } else {
             __syncthreads();
-            M[0] = s_max[0];
-            M[1] = s_max[1];
         }
-        acc_bind(fix, fw, hcnt, fdig);
+        fix.cnt = hcnt;
+        fix.dig = fdig;
         fix.flag = fflag;
         fix.sp = &s_spill;
         fix.S = Sa;
-        fix.scale[0] = fix_scale(M[0]);
-        fix.scale[1] = fix_scale(M[1]);
     }
 
     // ---- the warp's full tiles.  The loop runs the CTA's count so that
@@ -621,9 +548,7 @@ stream_kernel(const __grid_constant__ StreamProg sp,
     // pace.
     constexpr int kStore = stream_store_bits<SHAPE>() | (PK ? 0x0A : 0);
     constexpr int kLoad = stream_load_bits<SHAPE, PK, ACC>();
-    constexpr int kFlushEvery =
-        (int)((kStreamWords ? kFix64MaxPerCta : kFixMaxPerCta) /
-              (kStreamWarps * kStreamTile));
+    constexpr int kFlushEvery = (int)(kFixMaxPerCta / (kStreamWarps * kStreamTile));
     volatile int* abort_flag = &s_abort;
     int st = 0;
     unsigned ph = 0u;
@@ -662,7 +587,7 @@ stream_kernel(const __grid_constant__ StreamProg sp,
         if constexpr (ACC) {
             if ((k + 1) % kFlushEvery == 0) {
                 __syncthreads();
-                acc_flush(fix, PL + column, tid, kStreamThreads);
+                fix_flush(fix, tid, kStreamThreads);
                 __syncthreads();
             }
         }
@@ -712,7 +637,7 @@ stream_kernel(const __grid_constant__ StreamProg sp,
         }
         if (crank == 0) {
             for (int s = tid; s < Sa; s += kStreamThreads) {
-                long long c = kStreamWords ? __ldcg(PL + (int64_t)s * G + column) : 0;
+                long long c = 0;
                 long long tq[2];
                 unsigned fl = 0;
                 tq[0] = __ldcg(PL + (int64_t)(Sa + s) * G + column);
@@ -721,32 +646,24 @@ stream_kernel(const __grid_constant__ StreamProg sp,
                     const unsigned* rf = fflag;
                     if (clustered) rf = cg::this_cluster().map_shared_rank(fflag, r);
                     fl |= (rf[s >> 2] >> (8 * (s & 3))) & 0xffu;
-                    if constexpr (kStreamWords) {
-                        const unsigned long long* rw = fw;
-                        if (clustered) rw = cg::this_cluster().map_shared_rank(fw, r);
-                        long long n, sx;
-                        FixWords::split(rw[s], &n, &sx);
-                        c += n;
-                        tq[0] += sx;
-                        tq[1] += (long long)rw[Sa + s];
-                    } else {
-                        const int* rc = hcnt;
-                        const int* rd = fdig;
-                        if (clustered) {
-                            cg::cluster_group cl = cg::this_cluster();
-                            rc = cl.map_shared_rank(hcnt, r);
-                            rd = cl.map_shared_rank(fdig, r);
-                        }
-                        c += rc[s];
-#pragma unroll
-                        for (int q = 0; q < 2; ++q)
-                            tq[q] += FixHist::total(rd + 2 * q * Sa + s, Sa);
+                    const int* rc = hcnt;
+                    const int* rd = fdig;
+                    if (clustered) {
+                        cg::cluster_group cl = cg::this_cluster();
+                        rc = cl.map_shared_rank(hcnt, r);
+                        rd = cl.map_shared_rank(fdig, r);
                     }
+                    c += rc[s];
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+                        tq[q] += FixHist::total(rd + 2 * q * Sa + s, Sa);
                 }
                 P[(int64_t)s * G + column] = (double)c;
                 P[(int64_t)(Sa + s) * G + column] = fix_value(tq[0], fl & 15u, fix.scale[0]);
                 P[(int64_t)(2 * Sa + s) * G + column] = fix_value(tq[1], fl >> 4, fix.scale[1]);
             }
+            zero_spare_columns(P, Sa, G, column, (int)gridDim.x / (int)nb, tid,
+                               kStreamThreads);
         }
         if (clustered) cg::this_cluster().sync();
     }

@@ -26,9 +26,9 @@ from . import _native as N
 DEFAULT_PLAN = (-1, -1, -1)
 
 # (variant, stages, shared-memory KB): the tile-shared kernel (0) with the
-# TMA ring of 0 / 2 / 3 stages at four, three or two CTAs per SM, and the
-# streaming kernel (1) with 2-4 stages per warp
-CANDIDATES = ([(0, s, kb) for s in (0, 2, 3) for kb in (56, 72, 108)] +
+# TMA ring of 0 / 2 / 3 / 4 stages at four, three or two CTAs per SM, and
+# the streaming kernel (1) with 2-4 stages per warp
+CANDIDATES = ([(0, s, kb) for s in (0, 2, 3, 4) for kb in (56, 72, 108)] +
               [(1, s, kb) for s in (2, 3, 4) for kb in (56, 72, 108)])
 
 _state = {'enabled': False, 'cache_path': None, 'cache': None,
