@@ -513,33 +513,71 @@ stream_kernel(const __grid_constant__ StreamProg sp,
 
     FixHist fix;
     if constexpr (ACC) {
-        // ---- the fixed-point scales (the same in every CTA of every
-        // launch shape), then rank 0 clears its column's level-B sums
-        // before any member of the cluster adds to them
-        fix_sample_scales(a.c[PHK_X], a.c[PHK_Y], a.n, s_max, tid,
-                          kStreamThreads, fix.scale);
+        // ---- the cluster's fixed-point scale, from each warp's first tile
+        unsigned m[2] = {0u, 0u};
+        auto see = [&](float u, int q) {
+            const unsigned b = __float_as_uint(u) & 0x7fffffffu;
+            if (b < 0x7f800000u && b > m[q]) m[q] = b;
+        };
+        if (mine > 0) {
+            bad = !mbar_wait(wb, 0u, a.wait_limit);
+            if (!bad) {
+                const float* src = ring + lane * 2;
+                see(src[PHK_X * kStreamTile], 0);
+                see(src[PHK_X * kStreamTile + 1], 0);
+                see(src[PHK_Y * kStreamTile], 1);
+                see(src[PHK_Y * kStreamTile + 1], 1);
+            }
+        } else if (has_partial) {
+            const int64_t i0 = (int64_t)n_full * kStreamTile + lane * 2;
+            for (int j = 0; j < 2; ++j) {
+                if (i0 + j < a.n) {
+                    see(a.c[PHK_X][i0 + j], 0);
+                    see(a.c[PHK_Y][i0 + j], 1);
+                }
+            }
+        }
+        m[0] = __reduce_max_sync(0xffffffffu, m[0]);
+        m[1] = __reduce_max_sync(0xffffffffu, m[1]);
+        if (lane == 0) {
+            atomicMax(&s_max[0], m[0]);
+            atomicMax(&s_max[1], m[1]);
+        }
         if (tid == 0) {
             s_spill.spill[0] = PL + (int64_t)Sa * G + column;
             s_spill.spill[1] = PL + (int64_t)2 * Sa * G + column;
             s_spill.stride = G;
         }
         if (crank == 0) {
+            // the level-B sums of the column start at zero
             for (int s = tid; s < Sa; s += kStreamThreads) {
                 PL[(int64_t)(Sa + s) * G + column] = 0;
                 PL[(int64_t)(2 * Sa + s) * G + column] = 0;
             }
         }
+        unsigned M[2];
         if (clustered) {
             __threadfence();
-            cg::this_cluster().sync();
+            cg::cluster_group cl = cg::this_cluster();
+            cl.sync();
+            M[0] = M[1] = 0u;
+            for (unsigned r = 0; r < cl.num_blocks(); ++r) {
+                const unsigned* sm = cl.map_shared_rank(s_max, r);
+                M[0] = max(M[0], sm[0]);
+                M[1] = max(M[1], sm[1]);
+            }
         } else {
             __syncthreads();
+            M[0] = s_max[0];
+            M[1] = s_max[1];
         }
         fix.cnt = hcnt;
         fix.dig = fdig;
         fix.flag = fflag;
         fix.sp = &s_spill;
         fix.S = Sa;
+        fix.scale[0] = fix_scale(M[0]);
+        fix.scale[1] = fix_scale(M[1]);
     }
 
     // ---- the warp's full tiles.  The loop runs the CTA's count so that
@@ -662,8 +700,6 @@ stream_kernel(const __grid_constant__ StreamProg sp,
                 P[(int64_t)(Sa + s) * G + column] = fix_value(tq[0], fl & 15u, fix.scale[0]);
                 P[(int64_t)(2 * Sa + s) * G + column] = fix_value(tq[1], fl >> 4, fix.scale[1]);
             }
-            zero_spare_columns(P, Sa, G, column, (int)gridDim.x / (int)nb, tid,
-                               kStreamThreads);
         }
         if (clustered) cg::this_cluster().sync();
     }

@@ -877,10 +877,9 @@ __device__ __forceinline__ void warp_accumulate(int s, T vx, T vy,
 // -------------------------------------------------------------------
 // FixHist: exact, order-independent per-slice sums of FP32 coordinates.
 //
-// Every CTA uses one power-of-two scale per coordinate, 2^k with k chosen
-// from the largest finite |u| of 512 particles spread over the bunch (16
-// runs of 32) so that it maps to [2^26, 2^27) (the same scale whatever the
-// grid).  A value
+// Every thread-block cluster agrees on one power-of-two scale per
+// coordinate, 2^k with k chosen from the largest finite |u| of the
+// cluster's first tiles so that it maps to [2^26, 2^27).  A value
 // u becomes the integer v = rint(u 2^k) (u 2^k is exact; the rounding is
 // the only approximation, at most 2^-27 of that largest value, the order
 // of the FP32 rounding of u itself).  Level A, |u 2^k| < 2^30: v is split into two
@@ -965,41 +964,6 @@ __device__ __forceinline__ float fix_scale(unsigned mbits) {
     }
     k = k > 100 ? 100 : (k < -100 ? -100 : k);
     return ldexpf(1.0f, k);
-}
-
-// The fixed-point scales of a pass: 2^k for x and y (fix_scale) from the
-// largest finite |x|, |y| among kFixSample particles spread over the bunch
-// in 16 runs of 32 (run r starts at particle r n / 16; every particle of a
-// smaller bunch), each run one coalesced warp load.  Every CTA of every
-// launch shape and kernel variant computes the same scales, so the sums do
-// not depend on the grid.  All threads of the CTA call this (s_max zeroed
-// before); it synchronises the CTA.
-constexpr int kFixSample = 512;
-__device__ __forceinline__ int64_t fix_sample_index(int64_t t, int64_t n) {
-    return n <= kFixSample ? t : (t >> 5) * n / (kFixSample / 32) + (t & 31);
-}
-__device__ __forceinline__ void fix_sample_scales(const float* x, const float* y,
-                                                  int64_t n, unsigned* s_max,
-                                                  int tid, int nthreads,
-                                                  float* scale) {
-    unsigned m[2] = {0u, 0u};
-    const int64_t lim = n < kFixSample ? n : kFixSample;
-    for (int64_t t = tid; t < lim; t += nthreads) {
-        const int64_t i = fix_sample_index(t, n);
-        const unsigned bx = __float_as_uint(x[i]) & 0x7fffffffu;
-        const unsigned by = __float_as_uint(y[i]) & 0x7fffffffu;
-        if (bx < 0x7f800000u && bx > m[0]) m[0] = bx;
-        if (by < 0x7f800000u && by > m[1]) m[1] = by;
-    }
-    m[0] = __reduce_max_sync(0xffffffffu, m[0]);
-    m[1] = __reduce_max_sync(0xffffffffu, m[1]);
-    if ((tid & 31) == 0) {
-        atomicMax(&s_max[0], m[0]);
-        atomicMax(&s_max[1], m[1]);
-    }
-    __syncthreads();
-    scale[0] = fix_scale(s_max[0]);
-    scale[1] = fix_scale(s_max[1]);
 }
 
 // the FP64 value of a slice sum from its 64-bit total and flag nibble
@@ -1454,10 +1418,7 @@ __device__ __forceinline__ void load_tile_plain(const TrackArgs& a,
 // FP32 single-bunch kernel: particles per thread, resident CTAs per SM it
 // is compiled for (register cap) and the shared memory a CTA may plan for
 constexpr int kF32Vec = 2;
-#ifndef PHK_F32_MIN_BLOCKS
-#define PHK_F32_MIN_BLOCKS 4
-#endif
-constexpr int kF32MinBlocks = PHK_F32_MIN_BLOCKS;
+constexpr int kF32MinBlocks = 4;
 constexpr size_t kF32SmemBudget = 56 * 1024;
 constexpr size_t kF64SmemBudget = 112 * 1024;
 
@@ -1465,17 +1426,6 @@ constexpr size_t kF64SmemBudget = 112 * 1024;
 constexpr unsigned kWaitLimit = 1u << 22;
 // stages of the TMA ring at most
 constexpr int kMaxStages = 4;
-
-// A launch of fewer clusters than the workspace has partial columns (a
-// launch plan with fewer resident CTAs per SM) zeroes the columns that no
-// cluster of it owns, so that merging every column sees this launch's sums
-// only.  Called by the rank-0 CTA of each cluster.
-__device__ __forceinline__ void zero_spare_columns(double* P, int Sa, int G,
-                                                   int column, int launched,
-                                                   int tid, int nthreads) {
-    for (int col = column + launched; col < G; col += launched)
-        for (int i = tid; i < 3 * Sa; i += nthreads) P[(int64_t)i * G + col] = 0.0;
-}
 
 // FixHist counters are added to the level-B column after this many tiles
 // of a CTA (kFixMaxPerCta values per counter at most)
@@ -1615,34 +1565,79 @@ track_kernel(const __grid_constant__ phk_program prog,
 
     if constexpr (FIX) {
         if (a.has_acc) {
-            // ---- the fixed-point scales (the same in every CTA of every
-            // launch shape), then rank 0 clears its column's level-B sums
-            // before any member of the cluster adds to them
-            fix_sample_scales(reinterpret_cast<const float*>(a.c[PHK_X]),
-                              reinterpret_cast<const float*>(a.c[PHK_Y]), a.n,
-                              s_max, tid, blockDim.x, cx.fix.scale);
+            // ---- the cluster's scale: largest finite |x|, |y| of the inputs
+            // of every member's first tile (the maps change them by factors
+            // of order one; larger values take level B)
+            unsigned m[2] = {0u, 0u};
+            auto see = [&](float u, int q) {
+                const unsigned b = __float_as_uint(u) & 0x7fffffffu;
+                if (b < 0x7f800000u && b > m[q]) m[q] = b;
+            };
+            if (mine > 0) {
+                bad = !mbar_wait(bars, 0u, a.wait_limit);
+                if (!bad) {
+                    const T* src = ring + tid * VEC;
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) {
+                        see(src[(size_t)PHK_X * TILE + j], 0);
+                        see(src[(size_t)PHK_Y * TILE + j], 1);
+                    }
+                }
+            } else {
+                const int64_t i0 = (a.stages > 0 ? full_tiles * TILE
+                                                 : (int64_t)blockIdx.x * TILE) +
+                                   tid * VEC;
+                if (a.stages == 0 || has_partial) {
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) {
+                        if (i0 + j < a.n) {
+                            see(cx.cp[PHK_X][i0 + j], 0);
+                            see(cx.cp[PHK_Y][i0 + j], 1);
+                        }
+                    }
+                }
+            }
+            m[0] = __reduce_max_sync(0xffffffffu, m[0]);
+            m[1] = __reduce_max_sync(0xffffffffu, m[1]);
+            if ((tid & 31) == 0) {
+                atomicMax(&s_max[0], m[0]);
+                atomicMax(&s_max[1], m[1]);
+            }
             if (tid == 0) {
                 s_spill.spill[0] = reinterpret_cast<long long*>(P) + (int64_t)Sa * G + column;
                 s_spill.spill[1] = reinterpret_cast<long long*>(P) + (int64_t)2 * Sa * G + column;
                 s_spill.stride = G;
             }
+            // rank 0 clears its column's level-B sums before any member adds
             if (crank == 0) {
                 for (int s = tid; s < Sa; s += blockDim.x) {
                     reinterpret_cast<long long*>(P)[(int64_t)(Sa + s) * G + column] = 0;
                     reinterpret_cast<long long*>(P)[(int64_t)(2 * Sa + s) * G + column] = 0;
                 }
             }
+            unsigned M[2];
             if (clustered) {
                 __threadfence();
-                cg::this_cluster().sync();
+                cg::cluster_group cl = cg::this_cluster();
+                cl.sync();
+                M[0] = M[1] = 0u;
+                for (unsigned r = 0; r < cl.num_blocks(); ++r) {
+                    const unsigned* sm = cl.map_shared_rank(s_max, r);
+                    M[0] = max(M[0], sm[0]);
+                    M[1] = max(M[1], sm[1]);
+                }
             } else {
                 __syncthreads();
+                M[0] = s_max[0];
+                M[1] = s_max[1];
             }
             cx.fix.cnt = hcnt;
             cx.fix.dig = fdig;
             cx.fix.flag = fflag;
             cx.fix.sp = &s_spill;
             cx.fix.S = Sa;
+            cx.fix.scale[0] = fix_scale(M[0]);
+            cx.fix.scale[1] = fix_scale(M[1]);
         }
     }
 
@@ -1792,8 +1787,6 @@ track_kernel(const __grid_constant__ phk_program prog,
                 P[(int64_t)(2 * Sa + s) * G + column] =
                     fix_value(tq[1], fl >> 4, cx.fix.scale[1]);
             }
-            zero_spare_columns(P, Sa, G, column, (int)gridDim.x / (int)nb, tid,
-                               blockDim.x);
         }
         if (clustered) cg::this_cluster().sync();  // members keep their counters until read
         return;
@@ -1835,9 +1828,6 @@ track_kernel(const __grid_constant__ phk_program prog,
             P[(int64_t)(Sa + s) * G + column] = Hist<T>::value(hsx + s);
             P[(int64_t)(2 * Sa + s) * G + column] = Hist<T>::value(hsy + s);
         }
-        zero_spare_columns(P, Sa, G, column,
-                           (int)gridDim.x / (clustered ? a.cluster : 1), tid,
-                           blockDim.x);
     }
 }
 
@@ -2006,24 +1996,12 @@ static int occupancy_clusters(size_t smem) {
     return n < 1 ? 1 : n;
 }
 
-// occupancy_clusters of the last shared-memory size asked for, per device
-template <typename T, int VEC, int SHAPE>
-static int resident_clusters(size_t smem) {
-    static size_t last_smem[64];
-    static int last_n[64];
-    const int dev = device_info().device < 64 ? device_info().device : 63;
-    if (last_n[dev] == 0 || last_smem[dev] != smem) {
-        last_n[dev] = occupancy_clusters<T, VEC, SHAPE>(smem);
-        last_smem[dev] = smem;
-    }
-    return last_n[dev];
-}
-
 template <typename T, int VEC, int SHAPE>
 static int launch_track_t(const phk_program* prog, const phk_coords* c,
                           const phk_kick_set* pk, const phk_accum* acc,
                           int load_mask, int store_mask, cudaStream_t st) {
     TrackArgs a;
+    memset(&a, 0, sizeof(a));
     a.c[0] = c->x; a.c[1] = c->xp; a.c[2] = c->y;
     a.c[3] = c->yp; a.c[4] = c->z; a.c[5] = c->dp;
     a.n = c->n;
@@ -2061,14 +2039,10 @@ static int launch_track_t(const phk_program* prog, const phk_coords* c,
     prepare_track_kernel<T, VEC, SHAPE>();
     cudaError_t e;
     if (acc) {
-        // one partial column per cluster of kCluster CTAs, as many clusters
-        // as are resident with this plan's shared memory (at most one per
-        // column)
+        // one partial column per cluster of kCluster CTAs
         a.cluster = kCluster;
-        int clusters = resident_clusters<T, VEC, SHAPE>(smem);
-        if (clusters > acc->grid) clusters = acc->grid;
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)clusters * kCluster, 1, 1);
+        cfg.gridDim = dim3((unsigned)acc->grid * kCluster, 1, 1);
         cfg.blockDim = dim3(kTrackThreads, 1, 1);
         cfg.dynamicSmemBytes = smem;
         cfg.stream = st;

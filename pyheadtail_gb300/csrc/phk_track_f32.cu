@@ -3,36 +3,6 @@
 
 namespace phk {
 
-// clusters of the streaming kernel resident with `smem` (last size asked
-// for, per device)
-template <int SHAPE, bool PK, bool ACC>
-static int stream_resident_clusters(size_t smem) {
-    static size_t last_smem[64];
-    static int last_n[64];
-    const int dev = device_info().device < 64 ? device_info().device : 63;
-    if (last_n[dev] != 0 && last_smem[dev] == smem) return last_n[dev];
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kCluster * device_info().sm_count, 1, 1);
-    cfg.blockDim = dim3(kStreamThreads, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute attr;
-    attr.id = cudaLaunchAttributeClusterDimension;
-    attr.val.clusterDim.x = kCluster;
-    attr.val.clusterDim.y = 1;
-    attr.val.clusterDim.z = 1;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
-    int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, stream_kernel<SHAPE, PK, ACC>, &cfg) !=
-            cudaSuccess || n < 1) {
-        cudaGetLastError();
-        n = device_info().sm_count / kCluster;
-    }
-    last_n[dev] = n < 1 ? 1 : n;
-    last_smem[dev] = smem;
-    return last_n[dev];
-}
-
 template <int SHAPE, bool PK, bool ACC>
 static int launch_stream_t(const StreamProg& sp, const phk_coords* c,
                            const phk_kick_set* pk, const phk_accum* acc,
@@ -59,10 +29,8 @@ static int launch_stream_t(const StreamProg& sp, const phk_coords* c,
     cudaError_t e;
     if (ACC) {
         // one partial column per cluster of kCluster CTAs
-        int clusters = stream_resident_clusters<SHAPE, PK, ACC>(smem);
-        if (clusters > acc->grid) clusters = acc->grid;
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)clusters * kCluster, 1, 1);
+        cfg.gridDim = dim3((unsigned)acc->grid * kCluster, 1, 1);
         cfg.blockDim = dim3(kStreamThreads, 1, 1);
         cfg.dynamicSmemBytes = smem;
         cfg.stream = st;

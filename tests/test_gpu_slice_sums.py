@@ -2,13 +2,10 @@
 on every launch.
 
 The fused kernel of the precision form accumulates x and y per slice as
-integers at a power-of-two scale that every CTA takes from the same 512
-particles spread over the bunch (16 runs of 32; their largest |u| maps to
-[2^26, 2^27)),
-so the only error is the rounding of each value to that scale: at most
-2^-27 of the largest |u| per value, the order of the FP32 rounding of the
-value itself, and the sums do not depend on the launch shape.  Checked
-here:
+integers at a power-of-two scale agreed by each thread-block cluster (the
+largest |u| of its first tiles maps to [2^26, 2^27)), so the only error is
+the rounding of each value to that scale: at most 2^-27 of the largest
+|u| per value, below the FP32 rounding of the value itself.  Checked here:
 
 * at the multi-turn wake workload's size (1e7 macroparticles, 500 slices)
   and at the large single bunch's (5e7, 1000 slices): repeated slicings of
@@ -16,8 +13,8 @@ here:
   coordinates, give bit-identical counts, means and coordinates;
 * the means equal the FP64 sums of the FP32 values within that bound;
 * values far above the scale (exact 64-bit path), NaN and +-inf (the
-  slice mean becomes NaN or +-inf as a floating-point sum would), and a
-  scale sample that is all zero.
+  slice mean becomes NaN or +-inf as a floating-point sum would), and
+  clusters whose first tiles are all zero.
 The reference sums each slice sequentially in FP64
 (cobra_functions/stats.pyx:235-253)."""
 import numpy as np
@@ -141,13 +138,13 @@ def _slice_and_reference(coords, n, S):
 
 
 def test_outliers_nan_and_inf():
-    """Values up to 2^14 times the largest |x| of the scale sample take the
-    exact 64-bit path; NaN and infinities make the slice mean NaN / +-inf as
-    a floating-point sum would (slice 20: NaN, 21: +inf, 22: both
-    infinities, 23: -inf)."""
+    """Values up to 2^14 times the largest |x| of the cluster's first tiles
+    take the exact 64-bit path; NaN and infinities make the slice mean NaN
+    / +-inf as a floating-point sum would (slice 20: NaN, 21: +inf, 22:
+    both infinities, 23: -inf)."""
     import cases as C
-    # the planted values are the last 20 particles, outside the 512 the
-    # scale is sampled from (the last run ends at particle 15 n / 16 + 31)
+    # several tiles per CTA: the last (partial) tile, which holds the
+    # planted values, belongs to a CTA whose first tile is ordinary
     n, S = 2 * 10**6 + 300, 50
     rng = np.random.RandomState(7)
     tail, head = C.Z_CUTS
@@ -175,21 +172,14 @@ def test_outliers_nan_and_inf():
     assert abs(got[10] - want[10]) <= 2.0**-27 * typical
 
 
-def _scale_sample(n):
-    """Indices of the 512 particles the fixed-point scale is taken from:
-    16 runs of 32, run r starting at particle r n / 16."""
-    t = np.arange(512, dtype=np.int64)
-    return (t >> 5) * n // 16 + (t & 31)
-
-
-def test_zero_scale_sample():
-    """The 512 particles the fixed-point scale is taken from hold x = 0, so
-    the data give no scale: every CTA falls back to 2^40 and the other
-    values take the exact level-B path."""
+def test_zero_first_tiles():
+    """Every CTA's first tile holds x = 0 (no scale from the data): the
+    clusters fall back to the scale 2^40, the later values take the exact
+    levels."""
     n, S = 2 * 10**6, 100
     rng = np.random.RandomState(8)
     x = rng.normal(0, 1e-3, n)
-    x[_scale_sample(n)] = 0.0
+    x[:600 * 512] = 0.0
     coords = dict(x=x, xp=rng.normal(0, 1e-5, n), y=rng.normal(0, 1e-3, n),
                   yp=rng.normal(0, 1e-5, n), z=rng.normal(0, 0.23, n),
                   dp=rng.normal(0, 1e-3, n))
