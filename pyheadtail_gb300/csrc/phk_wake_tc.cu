@@ -234,21 +234,22 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
     // samples of one table row in descending order: five aligned 32-bit
     // loads, four byte permutes, one 16-byte store in the canonical
     // layout.  Thread t fills segment t & 7 of rows (t >> 3) + 32 m; rows
-    // past the slices and columns past the groups are zero.
+    // past the slices and columns past the groups are zero.  The loads of
+    // the next chunk are issued right after a tile's stores, so they are
+    // in flight while the CTA synchronises and its MMAs are issued.
     const int SC = lag_cols(S), Ls = row_stride(S);
     const int k_valid = w.group_k0[w.n_groups - 1] + w.group_lags[w.n_groups - 1] * SC;
     const unsigned* thi = reinterpret_cast<const unsigned*>(w.a_hi);
     const unsigned* tlo = reinterpret_cast<const unsigned*>(w.a_lo);
-    auto build = [&](int it, int st) {
+    constexpr int kRows = kTcM / kTcBuildRows;
+    // the source words of chunk c0 + it (loads only; held in registers so
+    // that their latency overlaps the previous chunk's barrier and MMAs)
+    auto build_load = [&](int it, unsigned (&h)[kRows][5], unsigned (&l)[kRows][5]) {
         const int c = tid & 7;
         const int kg0 = (c0 + it) * kTcK + 8 * c;
         const int R = kg0 / SC;
         const int j0 = kg0 - R * SC;
         const bool cols = kg0 < k_valid;
-        unsigned char* dst = smem + st * kStage;
-        constexpr int kRows = kTcM / kTcBuildRows;
-        unsigned h[kRows][5], l[kRows][5];
-        // every load of the tile first (one round trip), then the permutes
 #pragma unroll
         for (int m = 0; m < kRows; ++m) {
             const int i = mt * kTcM + (tid >> 3) + kTcBuildRows * m;
@@ -262,6 +263,15 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
                 l[m][q] = on ? __ldg(tlo + w0 + q) : 0u;
             }
         }
+    };
+    // the permutes and stores of chunk c0 + it into stage st
+    auto build_store = [&](int it, int st, const unsigned (&h)[kRows][5],
+                           const unsigned (&l)[kRows][5]) {
+        const int c = tid & 7;
+        const int kg0 = (c0 + it) * kTcK + 8 * c;
+        const int R = kg0 / SC;
+        const int j0 = kg0 - R * SC;
+        unsigned char* dst = smem + st * kStage;
 #pragma unroll
         for (int m = 0; m < kRows; ++m) {
             const int r = (tid >> 3) + kTcBuildRows * m;
@@ -278,6 +288,8 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
             *reinterpret_cast<uint4*>(dst + kTcTileBytes + off) = vl;
         }
     };
+    unsigned src_h[kRows][5], src_l[kRows][5];
+    if (nc > 0) build_load(0, src_h, src_l);    // in flight during B staging
 
     // B of every chunk of this CTA: one K column per thread and pass,
     // decoded once, then the rows of its kicks (hi rows 0..nk-1, lo rows
@@ -318,7 +330,8 @@ wake_gemm_kernel(const __grid_constant__ phk_wake_tc w, unsigned wait_limit) {
             break;
         }
         tc_fence_after_sync();
-        build(it, st);
+        build_store(it, st, src_h, src_l);
+        if (it + 1 < nc) build_load(it + 1, src_h, src_l);
         fence_proxy_async_smem();      // generic writes -> tensor-core reads
         __syncthreads();
         if (tid == 0) {
