@@ -98,6 +98,36 @@ def test_batch_matches_oracle_bunch_by_bunch(lib):
             <= 1e-12
 
 
+def test_batch_large_bunches_match_oracle(lib):
+    """Bunches at the top of the batched workload's size range (1e6
+    macroparticles, as the largest of its log-uniform draw in [1e4, 1e6])
+    beside mid-size and ragged ones, each with its own Q' and intensity:
+    the oracle bunch by bunch after 6 turns, counts exact, coordinates and
+    slice means within 1e-12."""
+    from oracle import cases as OC
+    T = 6
+    specs = _specs([1000000, 370001, 12345], T, seed=90)
+    coords = [_coords(s) for s in specs]
+    beams, turn = _batched(specs, coords)
+    turn.track(T)
+    torch.cuda.synchronize()
+    assert turn.read_status() == 0
+    p = 't%d_e2_' % (T - 1)
+    for b, spec in enumerate(specs):
+        ref = OC.run(spec, OC.make_beam(spec['beam']), n_turns=T,
+                     record_turns=(T - 1,))
+        got = beams[b].coords_numpy()
+        for k in COORDS:
+            assert rms_err(got[k], ref['t%d_%s' % (T - 1, k)]) <= 1e-12, \
+                (b, k)
+        np.testing.assert_array_equal(turn.counts[b].cpu().numpy(),
+                                      ref[p + 'counts'])
+        assert rms_err(turn.mean_x[b].cpu().numpy(), ref[p + 'mean_x']) \
+            <= 1e-12
+        assert rms_err(turn.mean_y[b].cpu().numpy(), ref[p + 'mean_y']) \
+            <= 1e-12
+
+
 @pytest.mark.parametrize('precision,tol', [('fp64', 1e-12), ('fp32', 1e-5)])
 def test_batch_matches_single_bunch_path(lib, precision, tol):
     import gpu_cases as G
