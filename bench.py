@@ -530,7 +530,12 @@ def run_ours(a, rank, world):
                          'traffic': None if tpp is None else tpp * w['n'],
                          'kernel': r['launch']['kernel'],
                          'kernel_ms': track_avg,
-                         'algorithmic_bytes_per_launch': bytes_pp * w['n']},
+                         'algorithmic_bytes_per_launch': bytes_pp * w['n'],
+                         'note': ('HBM fraction of a kernel bound by the FP64 '
+                                  'pipe (GB300 runs FP64 at 1/59 of the FP32 '
+                                  'rate); forms.fp32 is the HBM-bound form'
+                                  if precision == 'fp64' else
+                                  'HBM-bound form')},
             'e2e': {'value': w['n'] * r['e2e_turns_per_step'] *
                     len(r['e2e_s']) / e2e_t,
                     'unit': 'macroparticle-turns/s',
