@@ -1415,6 +1415,9 @@ __device__ __forceinline__ void load_tile_plain(const TrackArgs& a,
     }
 }
 
+// CTAs per thread-block cluster of an accumulating launch
+constexpr int kCluster = 4;
+
 // FP32 single-bunch kernel: particles per thread, resident CTAs per SM it
 // is compiled for (register cap) and the shared memory a CTA may plan for
 constexpr int kF32Vec = 2;
@@ -1765,7 +1768,11 @@ track_kernel(const __grid_constant__ phk_program prog,
                 unsigned fl = 0;
                 tq[0] = __ldcg(lp + (int64_t)(Sa + s) * G + column);
                 tq[1] = __ldcg(lp + (int64_t)(2 * Sa + s) * G + column);
-                for (unsigned r = 0; r < nb; ++r) {
+                // unrolled over the cluster's members, so that the loads of
+                // every member are in flight together
+#pragma unroll
+                for (int r = 0; r < kCluster; ++r) {
+                    if (r >= (int)nb) break;
                     const int* rc = hcnt;
                     const int* rd = fdig;
                     const unsigned* rf = fflag;
@@ -1959,8 +1966,6 @@ static size_t track_dynamic_smem_limit() {
     return (size_t)device_info().max_smem_optin - fa.sharedSizeBytes;
 }
 
-// CTAs per thread-block cluster of an accumulating launch
-constexpr int kCluster = 4;
 
 template <typename T, int VEC, int SHAPE>
 static int occupancy_blocks(size_t smem) {
