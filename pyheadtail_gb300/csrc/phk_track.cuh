@@ -1423,6 +1423,8 @@ constexpr int kCluster = 4;
 constexpr int kF32Vec = 2;
 constexpr int kF32MinBlocks = 4;
 constexpr size_t kF32SmemBudget = 56 * 1024;
+// shared memory a CTA may use at three CTAs per SM
+constexpr size_t kF32SmemBudget3 = 75 * 1024;
 constexpr size_t kF64SmemBudget = 112 * 1024;
 
 // polls of one mbarrier phase before a kernel gives up (order of a second)
@@ -1871,6 +1873,21 @@ static size_t smem_for(int Sa, int Sp, int n_tables, bool tma, int* n_hist,
             *n_hist = nh;
             *stages = forced_stages;
             return b;
+        }
+    }
+    if (fix && tma && budget_in == 0 && forced_stages < 0) {
+        // FP32 default: two ring stages at four CTAs per SM; where they do
+        // not fit (about 700 slices and more), two stages at three CTAs
+        // per SM, measured faster than plain loads at 1000 slices
+        const size_t budgets[2] = {kF32SmemBudget, kF32SmemBudget3};
+        for (int bi = 0; bi < 2; ++bi) {
+            const size_t b = track_smem_layout<T>(Sa, Sp, 1, n_tables, *kicks_smem,
+                                                  2, tile, off, fix);
+            if (b <= budgets[bi]) {
+                *n_hist = 1;
+                *stages = 2;
+                return b;
+            }
         }
     }
     size_t smallest = 0;

@@ -109,11 +109,11 @@ def plan_for(engine, prog, coords, ks, ac, ops, kick, acc, stream):
     return plan
 
 
-def _last_variant():
+def _last_launch():
     v, s, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
     N.call('phk_last_track_launch', ctypes.byref(v), ctypes.byref(s),
            ctypes.byref(m))
-    return v.value
+    return v.value, s.value
 
 
 def _time_candidates(engine, prog, coords, ks, ac, stream, reps=3):
@@ -141,9 +141,10 @@ def _time_candidates(engine, prog, coords, ks, ac, stream, reps=3):
                 torch.cuda.synchronize()
                 if it:
                     times.append(e0.elapsed_time(e1))
-            # a plan whose shared memory does not fit runs the other kernel:
-            # only plans that launched as asked compete
-            if _last_variant() == cand[0]:
+            # a plan whose shared memory does not fit runs the other kernel
+            # or fewer ring stages: only plans that launched as asked compete
+            v, s = _last_launch()
+            if v == cand[0] and (cand[1] < 0 or s == cand[1]):
                 results[cand] = float(np.median(times))
     finally:
         N.call('phk_set_track_plan', *DEFAULT_PLAN)
