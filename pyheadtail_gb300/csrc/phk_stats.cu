@@ -17,7 +17,7 @@
 //     coordinates only (NQ a template parameter, so the FP64 form issues
 //     one FP64 add per coordinate and particle and nothing else);
 //   * stats_kernel: everything else (kicks, order 2, any alignment).
-// GB300 runs FP64 at ~1/64 of its FP32 rate, so the FP64 form of both is
+// GB300 runs FP64 at ~1/59 of its FP32 rate (measured), so the FP64 form of both is
 // bound by FP64 issue, not by HBM: every FP64 instruction per particle
 // costs ~17 us per 1e7 particles.
 //
