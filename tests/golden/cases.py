@@ -223,6 +223,20 @@ CASES = {
                               mode='uniform_charge'),
                        resonator(),
                        resistive_wall(n_turns_wake=1))]),
+    # the multi-turn wake workload (500 slices, resonator + 50-turn
+    # resistive wall, RF) and the large-bunch physics (Q' 2, amplitude
+    # detuning, 1000 slices, the same wakes) at fixture size
+    'c3_full': dict(
+        beam=beam_params(1000, 2), n_turns=8,
+        elements=[smooth_transverse(), rf(),
+                  wake(slicer(500), resonator(),
+                       resistive_wall(n_turns_wake=50))]),
+    'c5_full': dict(
+        beam=beam_params(1000, 4), n_turns=5,
+        elements=[smooth_transverse(chroma=[2., 2.],
+                                    amplitude=[1e-11, 1e-11, -5e-12]),
+                  rf(), wake(slicer(1000), resonator(),
+                             resistive_wall(n_turns_wake=50))]),
     'c1_full': dict(
         beam=beam_params(1000, 0), n_turns=5,
         elements=[smooth_transverse(), linear_map(),

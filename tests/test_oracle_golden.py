@@ -50,6 +50,7 @@ def test_fixture_set_covers_every_stage():
                  'linear_map', 'rf_double_harmonic', 'rf_accelerating',
                  'slicer_fixed', 'wake_resonator', 'wake_multiturn',
                  'wake_dynamic_cuts', 'wake_plates', 'c1_full', 'c2_full',
+                 'c3_full', 'c5_full',
                  'bunch_statistics', 'wake_table_multiturn',
                  'wake_table_lowbeta', 'damper_resistive',
                  'damper_reactive', 'charge_slicer', 'wake_charge_slicer'):
