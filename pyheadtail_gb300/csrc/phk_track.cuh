@@ -783,7 +783,10 @@ __device__ __forceinline__ void run_program_shape(const phk_program& prog,
 //   lane order and the sums do not depend on scheduling.  FP64: plain
 //   double sums; FP32 (batched kernel): Kahan (1965) compensated float sums,
 //   one (sum, compensation) float2 per bin.  When the per-warp copies do not
-//   fit the shared-memory plan, warps share copies through atomics.
+//   fit the shared-memory plan, warps share copies through atomics; the
+//   order of the warps sharing a copy is then not fixed, so those sums can
+//   differ in their last bits between launches (FP64 single bunch: beyond
+//   511 slices with two kick tables, 573 without).
 //
 // FP32 single-bunch kernel: exact fixed-point sums (FixHist below), one
 //   histogram per CTA updated with 32-bit integer atomics: integer addition
