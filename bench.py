@@ -428,6 +428,33 @@ def _time_form(w, coords, precision, steps, warmup, flush, tune):
                 launch=launch)
 
 
+def host_cpu():
+    """The host the CPU baseline ran on: architecture, CPU model (x86
+    'model name', or the Arm implementer / part codes), logical CPUs and
+    the thread settings of the numerical libraries.  Never raises."""
+    import platform
+    out = {'machine': platform.machine(), 'logical_cpus': os.cpu_count(),
+           'OMP_NUM_THREADS': os.environ.get('OMP_NUM_THREADS'),
+           'OPENBLAS_NUM_THREADS': os.environ.get('OPENBLAS_NUM_THREADS')}
+    model = None
+    try:
+        fields = {}
+        with open('/proc/cpuinfo') as f:
+            for line in f:
+                if ':' in line:
+                    k, v = line.split(':', 1)
+                    fields.setdefault(k.strip(), v.strip())
+        if 'model name' in fields:
+            model = fields['model name']
+        elif 'CPU part' in fields:
+            model = 'implementer %s part %s' % (
+                fields.get('CPU implementer', '?'), fields['CPU part'])
+    except (OSError, ValueError):
+        pass
+    out['model'] = model or platform.processor() or None
+    return out
+
+
 def cpu_baseline(w, coords, budget_s=12.0):
     """Oracle (NumPy restatement of the reference) on the host, 1 thread,
     on a bounded sample: the full bunch (up to 1e7 particles), turns until
@@ -448,7 +475,7 @@ def cpu_baseline(w, coords, budget_s=12.0):
             break
     dt = time.perf_counter() - t0
     return {'value': ns * turns / dt, 'unit': 'macroparticle-turns/s',
-            'cores': 1, 'kind': 'port',
+            'cores': 1, 'kind': 'port', 'host': host_cpu(),
             'sample': '%d macroparticles x %d turns of the same workload '
                       '(oracle: NumPy restatement of the reference, single '
                       'thread, like the reference)' % (ns, turns)}
@@ -946,7 +973,7 @@ def run_batch(a, rank, world):
         v, tot, turns, nbs, procs = c4_oracle_sample()
         out['cpu_baseline'] = {
             'value': v, 'unit': 'macroparticle-turns/s', 'cores': procs,
-            'kind': 'port',
+            'kind': 'port', 'host': host_cpu(),
             'sample': '%d macroparticles (%d bunches of the batch, one '
                       'process per core) x >= %d turns (oracle)'
                       % (tot, nbs, turns)}
@@ -974,7 +1001,8 @@ def run_reference_c4(a, rank, world):
         'config': {'workload': C4['label'], 'n_bunches': C4['n_bunches'],
                    'n_slices': C4['slices'], 'form': 'fp64'},
         'cpu_baseline': {'value': v, 'unit': 'macroparticle-turns/s',
-                         'cores': procs, 'kind': 'port', 'sample': sample},
+                         'cores': procs, 'kind': 'port', 'sample': sample,
+                         'host': host_cpu()},
         'e2e': {'value': v, 'unit': 'macroparticle-turns/s',
                 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }))
@@ -1074,7 +1102,8 @@ def run_reference(a, rank, world):
                 'draw order), no dataset',
         'config': bench_config(w), 'form': 'fp64', 'turns_per_step': 1,
         'cpu_baseline': {'value': v, 'unit': 'macroparticle-turns/s',
-                         'cores': 1, 'kind': 'port', 'sample': sample},
+                         'cores': 1, 'kind': 'port', 'sample': sample,
+                         'host': host_cpu()},
         'e2e': {'value': v, 'unit': 'macroparticle-turns/s',
                 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }))

@@ -71,6 +71,7 @@ def test_reference_arm_line_keeps_the_contract():
     cb = d['cpu_baseline']
     assert cb['value'] == d['value'] and cb['cores'] >= 1
     assert cb['kind'] in ('port', 'reference') and cb['sample']
+    assert cb['host']['logical_cpus'] >= 1 and cb['host']['machine']
     assert d['e2e'] == {'value': d['value'], 'unit': d['unit'],
                         'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
     env = dict(os.environ, WORLD_SIZE='2', RANK='1', LOCAL_RANK='1')
@@ -78,3 +79,22 @@ def test_reference_arm_line_keeps_the_contract():
                          cwd=ROOT, env=env)
     assert out.returncode == 0, out.stderr[-2000:]
     assert not [l for l in out.stdout.splitlines() if l.startswith('{')]
+
+
+def test_host_description_never_raises(monkeypatch):
+    """The CPU baseline's host record: architecture, logical CPUs and the
+    model from /proc/cpuinfo, or None when that cannot be read."""
+    import builtins
+    sys.path.insert(0, ROOT)
+    import bench
+    h = bench.host_cpu()
+    assert set(h) == {'machine', 'logical_cpus', 'model', 'OMP_NUM_THREADS',
+                      'OPENBLAS_NUM_THREADS'}
+    real_open = builtins.open
+
+    def no_cpuinfo(path, *a, **k):
+        if path == '/proc/cpuinfo':
+            raise OSError('unreadable')
+        return real_open(path, *a, **k)
+    monkeypatch.setattr(builtins, 'open', no_cpuinfo)
+    assert bench.host_cpu()['logical_cpus'] == h['logical_cpus']
