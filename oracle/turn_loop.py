@@ -15,8 +15,13 @@ the checker or the timed CPU baseline.  The GB300 product path never calls it.
 Every expression keeps the reference's operation order so that results are
 bit-identical to the reference's NumPy/Cython path.  That claim is pinned by
 ``tests/test_oracle_golden.py`` against fixtures produced by running the
-reference itself (``tests/golden/make_golden.py``).  Citations are
-``path:line`` inside the PyHEADTAIL source tree.
+reference itself (``tests/golden/make_golden.py``), by the reference's own
+instability tests replayed from its bunches and traces
+(``tests/test_oracle_reswall.py``, ``tests/test_oracle_bb_resonator.py``)
+and, where the reference's source tree is present, at the full size of the
+1e7- and 5e7-macroparticle workloads
+(``tests/golden/compare_full_size.py``).  Citations are ``path:line``
+inside the PyHEADTAIL source tree.
 """
 from collections import deque
 from math import factorial
