@@ -5,11 +5,13 @@
 //
 // Each warp streams its own warp-tiles of 64 particles (two per lane)
 // through a private ring of TMA bulk copies: no block-wide barrier and no
-// bookkeeping between warps in the loop.  The arithmetic is the scalar FP32
-// form of phk_track.cuh (operands from the parameter bank, no register
-// pairs to build), the stores are evict-first 8-byte stores at 32-bit
-// offsets, and the per-slice sums are the exact FixHist sums.  Launches
-// outside these cases run track_kernel.
+// bookkeeping between warps in the loop.  The arithmetic is the FP32 form
+// of phk_track.cuh on the paired FP32 pipes (a lane's two particles in one
+// instruction, each lane the same IEEE operation in the same order as the
+// scalar form, operands from the parameter bank); the partial last
+// warp-tile runs the scalar form particle by particle.  The stores are
+// evict-first 8-byte stores at 32-bit offsets, and the per-slice sums are
+// the exact FixHist sums.  Launches outside these cases run track_kernel.
 #pragma once
 
 #include "phk_track.cuh"
@@ -48,7 +50,8 @@ struct StreamProg {
 };
 
 // ---- scalar FP32 element arithmetic on parameter-bank operands (the
-// operations of the FP32 forms in phk_track.cuh)
+// operations of the FP32 forms in phk_track.cuh), for the partial last
+// warp-tile
 template <int OPI>
 __device__ __forceinline__ void sp_chroma(const StreamProg& sp, int d, int q,
                                           float dp, float& dq) {
@@ -334,7 +337,7 @@ constexpr int stream_load_bits() {
                                : (SHAPE == SHAPE_T ? (0x2F | ((PK || ACC) ? 0x10 : 0)) : 0x3F);
 }
 
-// shared memory: FixHist [count Sa | digits 6 Sa | flags], accumulation
+// shared memory: FixHist [count Sa | digits 4 Sa | flags], accumulation
 // edges [Sa + 1], pending-kick edges [Sp + 1], summed kick tables
 // [n_tables][Sp], rings [warps][stages][6][64] floats, mbarriers
 // [warps][stages]
