@@ -10,7 +10,9 @@ namespace phk {
 size_t track_smem_bytes(int32_t dtype, int32_t Sa, int32_t Sp) {
     int nh, ks, st;
     // a turn's pending kicks: four dipolar kicks (resonator and resistive
-    // wall, both planes), staged as one summed table per plane in FP32
+    // wall, both planes).  Launches stage one summed table per plane; the
+    // FP64 size is taken for all four tables, an upper bound (the launched
+    // grid is the caller's column count either way)
     return dtype == PHK_F64 ? smem_for<double>(Sa, Sp, 4, false, &nh, &ks, &st)
                             : smem_for<float>(Sa, Sp, 2, true, &nh, &ks, &st);
 }

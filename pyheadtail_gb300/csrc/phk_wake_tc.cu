@@ -20,7 +20,8 @@
 // A tiles in shared memory, in the canonical no-swizzle K-major layout of
 // the tensor-core operand, from a bfloat16 hi / lo copy of the tables
 // (written once per table change; C3: 200 KB, read from L2).  B is built
-// per chunk in shared memory from the FP64 moment ring.  The K range is
+// in shared memory from the FP64 moment ring for all of a CTA's K chunks
+// (at most kTcMaxChunks) before its first MMA.  The K range is
 // split across CTAs; a fixed-order FP64 reduction of the split partials
 // applies the factors.
 #include <cuda_bf16.h>
