@@ -232,6 +232,14 @@ typedef struct phk_kick_set {
  * its per-slice count / sum x / sum y to the partial column
  * partials[q * n_slices * grid + s * grid + column] (q = 0,1,2).  Use
  * phk_track_grid() for `grid`; size partials >= 3 * n_slices * grid.
+ * Reproducibility: FP32 values are summed exactly as integers at a
+ * power-of-two scale per cluster (each value rounds by at most 2^-27 of
+ * the largest |value| of the cluster's first tiles), so the columns are
+ * bit-identical on every launch and for every launch plan.  FP64 sums are
+ * bit-identical while every warp has a private histogram copy (up to 511
+ * slices with two summed kick tables, 573 without kicks, fewer with more
+ * tables); beyond that, warps share copies through atomics and the last
+ * bits may differ between launches.
  * idx_out (optional, int32[n]) receives the reference's slice index of
  * every particle (outside particles included; NaN -> INT32_MIN).        */
 typedef struct phk_accum {
