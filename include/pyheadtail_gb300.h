@@ -4,8 +4,10 @@
  * The library replaces the per-particle arithmetic of PyHEADTAIL's turn loop
  * (v1.16.5) behind plain C entry points: device pointers, sizes and POD
  * parameter blocks, no torch or C++ types.  Every call is asynchronous on the
- * caller's CUDA stream (passed as void*, a cudaStream_t), never allocates
- * device memory (all buffers belong to the caller) and returns an int status:
+ * caller's CUDA stream (passed as void*, a cudaStream_t), allocates no
+ * device memory at run time (every buffer belongs to the caller, except the
+ * fixed scratch array of phk_slice_noalloc, which is loaded with the
+ * library) and returns an int status:
  *   0      success
  *   < 0    argument error detected on the host before any launch
  *          (PHK_E* below); the message is available from phk_last_error()
