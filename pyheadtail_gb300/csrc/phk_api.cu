@@ -82,6 +82,14 @@ static int check_slicer(const phk_slicer* s, const char* who) {
     return PHK_OK;
 }
 
+// the kernels read the edge table with loads of the coordinate type
+static int check_edges(const phk_slicer* s, int32_t dtype, const char* who) {
+    if (reinterpret_cast<uintptr_t>(s->edges) % dsize(dtype))
+        return set_error(PHK_EALIGN, "%s: slicer edges not %zu-byte aligned",
+                         who, dsize(dtype));
+    return PHK_OK;
+}
+
 static int check_coords(const phk_coords* c, const char* who) {
     if (!c) return set_error(PHK_ENULL, "%s: coords is NULL", who);
     int r = check_dtype(c->dtype, who);
@@ -148,6 +156,7 @@ static int check_program(const phk_program* p, const char* who) {
 static int check_kicks(const phk_kick_set* k, int32_t dtype, const char* who) {
     int r = check_slicer(&k->slicer, who);
     if (r) return r;
+    if ((r = check_edges(&k->slicer, dtype, who))) return r;
     if (k->n_kicks < 0 || k->n_kicks > PHK_MAX_KICKS)
         return set_error(PHK_ESIZE, "%s: n_kicks %d outside [0, %d]", who,
                          k->n_kicks, PHK_MAX_KICKS);
@@ -249,6 +258,8 @@ int phk_track(const phk_program* program, const phk_coords* coords,
     if (pending && (r = check_kicks(pending, coords->dtype, "phk_track")))
         return r;
     if (acc && (r = check_accum(acc, "phk_track"))) return r;
+    if (acc && (r = check_edges(&acc->slicer, coords->dtype, "phk_track")))
+        return r;
     if (coords->n == 0 && !acc) return PHK_OK;
     return launch_track(program, coords, pending, acc, (cudaStream_t)stream);
 }
@@ -338,6 +349,7 @@ int phk_slice_moments(const phk_slicer* slicer, const void* z, int64_t n,
     int r = check_slicer(slicer, who);
     if (r) return r;
     if ((r = check_dtype(dtype, who))) return r;
+    if ((r = check_edges(slicer, dtype, who))) return r;
     if (n < 0) return set_error(PHK_ESIZE, "%s: n < 0", who);
     if (n_q < 0 || n_q > 3) return set_error(PHK_ESIZE, "%s: n_q %d", who, n_q);
     if (pass != 0 && pass != 1) return set_error(PHK_EPARAM, "%s: pass", who);
@@ -349,6 +361,13 @@ int phk_slice_moments(const phk_slicer* slicer, const void* z, int64_t n,
     for (int q = 0; q < n_q; ++q)
         if (n > 0 && !quantities[q])
             return set_error(PHK_ENULL, "%s: quantity %d is NULL", who, q);
+    if (reinterpret_cast<uintptr_t>(z) % dsize(dtype))
+        return set_error(PHK_EALIGN, "%s: z not %zu-byte aligned", who,
+                         dsize(dtype));
+    for (int q = 0; q < n_q; ++q)
+        if (reinterpret_cast<uintptr_t>(quantities[q]) % dsize(dtype))
+            return set_error(PHK_EALIGN, "%s: quantity %d not %zu-byte "
+                             "aligned", who, q, dsize(dtype));
     if (n == 0) return PHK_OK;
     return launch_moments(slicer, z, n, dtype, quantities, n_q, pass, means,
                           sums, counts, (cudaStream_t)stream);
@@ -394,6 +413,7 @@ int phk_track_batch(const phk_batch* batch, const phk_coords* coords,
     }
     if (acc) {
         if ((r = check_accum(acc, who))) return r;
+        if ((r = check_edges(&acc->slicer, coords->dtype, who))) return r;
         if (b.n_columns < 1 || acc->grid != b.n_columns)
             return set_error(PHK_EPARAM, "%s: acc->grid %d must equal "
                              "n_columns %d >= 1", who, acc->grid, b.n_columns);

@@ -68,6 +68,9 @@ extern "C" int phk_slice_noalloc(const phk_slicer* slicer,
         return set_error(PHK_ESIZE, "phk_slice_noalloc: n = %lld < 0",
                          (long long)coords->n);
     const size_t al = coords->dtype == PHK_F64 ? 8 : 4;
+    if (reinterpret_cast<uintptr_t>(slicer->edges) % al)
+        return set_error(PHK_EALIGN, "phk_slice_noalloc: slicer edges not "
+                         "%zu-byte aligned", al);
     const void* xyz[3] = {coords->x, coords->y, coords->z};
     for (int q = 0; q < 3; ++q) {
         if (coords->n > 0 && !xyz[q])

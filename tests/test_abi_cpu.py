@@ -337,3 +337,52 @@ def test_tuning_disabled_leaves_plan_untouched(tmp_path):
     finally:
         tuning.enable(on=False)
     assert not tuning.enabled()
+
+
+def test_misaligned_tables_rejected_on_host(lib):
+    """The kernels read slice edges, z and the moment quantities with loads
+    of the coordinate type: a pointer that is not aligned to it is an
+    argument error on the host (PHK_EALIGN), never a launch."""
+    from pyheadtail_gb300 import _native as N
+    L = N.load(build_if_missing=False)
+    c = N.Coords()
+    for i, f in enumerate(('x', 'xp', 'y', 'yp', 'z', 'dp')):
+        setattr(c, f, 4096 * (i + 1))
+    c.n, c.dtype = 100, N.PHK_F64
+    prog = N.Program()
+    sl = N.Slicer()
+    sl.n_slices, sl.edges = 10, 65536 + 4          # 4-byte aligned only
+    acc = N.Accum()
+    acc.slicer = sl
+    acc.partials, acc.grid, acc.partials_len = 131072, 1, 30
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(c), None,
+                       ctypes.byref(acc), None) == -3
+    assert 'edges' in N.last_error()
+    ks = N.KickSet()
+    ks.slicer = sl
+    ks.n_kicks, ks.target[0], ks.quad[0], ks.kick[0] = 1, N.COORD_INDEX['xp'], -1, 262144
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(c), ctypes.byref(ks),
+                       None, None) == -3
+    assert L.phk_kick(ctypes.byref(c), ctypes.byref(ks), None) == -3
+    # FP32 coordinates need only 4-byte alignment of the edges: the same
+    # slicer passes the check and the call stops at a later argument error
+    # (no sums array), still before any launch
+    q = (ctypes.c_void_p * 1)(4096)
+    assert L.phk_slice_moments(ctypes.byref(sl), 4096, 100, N.PHK_F32, q, 1,
+                               0, None, None, 16384, None) == -1
+    assert 'sums' in N.last_error()
+    noalloc_sl = N.Slicer()
+    noalloc_sl.n_slices, noalloc_sl.edges = 10, 65536 + 4
+    assert L.phk_slice_noalloc(ctypes.byref(noalloc_sl), ctypes.byref(c),
+                               8192, 16384, 32768, None) == -3
+    # phk_slice_moments: edges, z and quantities
+    sums, counts = 8192, 16384
+    assert L.phk_slice_moments(ctypes.byref(sl), 4096, 100, N.PHK_F64, q, 1,
+                               0, None, sums, counts, None) == -3
+    sl.edges = 65536
+    assert L.phk_slice_moments(ctypes.byref(sl), 4096 + 4, 100, N.PHK_F64, q,
+                               1, 0, None, sums, counts, None) == -3
+    q[0] = 4096 + 4
+    assert L.phk_slice_moments(ctypes.byref(sl), 4096, 100, N.PHK_F64, q, 1,
+                               0, None, sums, counts, None) == -3
+    assert 'quantity' in N.last_error()
