@@ -82,6 +82,16 @@ static int check_slicer(const phk_slicer* s, const char* who) {
     return PHK_OK;
 }
 
+// a device pointer that kernels read or write with loads / stores of
+// `align` bytes (NULL passes: optional outputs are checked where required)
+static int check_aligned(const void* ptr, size_t align, const char* who,
+                         const char* what) {
+    if (reinterpret_cast<uintptr_t>(ptr) % align)
+        return set_error(PHK_EALIGN, "%s: %s not %zu-byte aligned", who, what,
+                         align);
+    return PHK_OK;
+}
+
 // the kernels read the edge table with loads of the coordinate type
 static int check_edges(const phk_slicer* s, int32_t dtype, const char* who) {
     if (reinterpret_cast<uintptr_t>(s->edges) % dsize(dtype))
@@ -181,6 +191,7 @@ static int check_accum(const phk_accum* a, const char* who) {
     int r = check_slicer(&a->slicer, who);
     if (r) return r;
     if (!a->partials) return set_error(PHK_ENULL, "%s: partials is NULL", who);
+    if ((r = check_aligned(a->partials, 8, who, "partials"))) return r;
     if (a->grid < 1) return set_error(PHK_ESIZE, "%s: grid %d < 1", who,
                                       a->grid);
     const int64_t need = 3LL * a->slicer.n_slices * a->grid;
@@ -269,6 +280,12 @@ int phk_slice_finalize(const phk_accum* acc, int32_t* counts, double* mean_x,
     if (!acc) return set_error(PHK_ENULL, "phk_slice_finalize: acc is NULL");
     int r = check_accum(acc, "phk_slice_finalize");
     if (r) return r;
+    const char* who = "phk_slice_finalize";
+    if ((r = check_aligned(counts, 4, who, "counts")) ||
+        (r = check_aligned(mean_x, 8, who, "mean_x")) ||
+        (r = check_aligned(mean_y, 8, who, "mean_y")) ||
+        (r = check_aligned(moments_slot, 8, who, "moments_slot")))
+        return r;
     return launch_finalize(acc, counts, mean_x, mean_y, moments_slot,
                            (cudaStream_t)stream);
 }
@@ -294,6 +311,13 @@ int phk_slice_merge(const double* sums, int32_t n_shards, int32_t n_slices,
                          "[1, %d]", n_slices, PHK_MAX_SLICES);
     if (reinterpret_cast<uintptr_t>(sums) % 8)
         return set_error(PHK_EALIGN, "phk_slice_merge: sums not 8-byte aligned");
+    const char* who = "phk_slice_merge";
+    int r;
+    if ((r = check_aligned(counts, 4, who, "counts")) ||
+        (r = check_aligned(mean_x, 8, who, "mean_x")) ||
+        (r = check_aligned(mean_y, 8, who, "mean_y")) ||
+        (r = check_aligned(moments_slot, 8, who, "moments_slot")))
+        return r;
     return launch_slice_merge(sums, n_shards, n_slices, counts, mean_x, mean_y,
                               moments_slot, (cudaStream_t)stream);
 }
@@ -311,6 +335,7 @@ int phk_wake(const phk_wake_set* w, void* stream) {
     if (!w->moments) return set_error(PHK_ENULL, "phk_wake: moments is NULL");
     int r = check_dtype(w->out_dtype, "phk_wake");
     if (r) return r;
+    if ((r = check_aligned(w->moments, 8, "phk_wake", "moments"))) return r;
     for (int k = 0; k < w->n_kicks; ++k) {
         const phk_wake_kick& kk = w->kick[k];
         if (!kk.table || !kk.out)
@@ -323,6 +348,10 @@ int phk_wake(const phk_wake_set* w, void* stream) {
                              "%d-slot ring", k, kk.n_lags, w->ring_len);
         if (kk.dense != 0 && kk.dense != 1)
             return set_error(PHK_EPARAM, "phk_wake: kick %d dense flag", k);
+        if ((r = check_aligned(kk.table, 8, "phk_wake", "a kick table")) ||
+            (r = check_aligned(kk.out, dsize(w->out_dtype), "phk_wake",
+                               "a kick output")))
+            return r;
     }
     if (w->n_kicks == 0) return PHK_OK;
     return launch_wake(w, (cudaStream_t)stream);
@@ -391,6 +420,12 @@ int phk_track_batch(const phk_batch* batch, const phk_coords* coords,
                          who);
     int r = check_coords(coords, who);
     if (r) return r;
+    if ((r = check_aligned(b.units, 8, who, "units")) ||
+        (r = check_aligned(b.cta_first, 4, who, "cta_first")) ||
+        (r = check_aligned(b.programs, 8, who, "programs")) ||
+        (r = check_aligned(b.kicks, dsize(coords->dtype), who, "kicks")) ||
+        (r = check_aligned(b.status, 4, who, "status")))
+        return r;
     const void* p[6] = {coords->x, coords->xp, coords->y, coords->yp,
                         coords->z, coords->dp};
     for (int q = 0; q < 6; ++q)
@@ -455,6 +490,12 @@ int phk_batch_finalize(const phk_accum* acc, int32_t n_bunches,
     if (moments && moments_stride < 3LL * acc->slicer.n_slices)
         return set_error(PHK_EPARAM, "%s: moments_stride %lld < 3 * n_slices",
                          who, (long long)moments_stride);
+    if ((r = check_aligned(bunch_columns, 4, who, "bunch_columns")) ||
+        (r = check_aligned(counts, 4, who, "counts")) ||
+        (r = check_aligned(mean_x, 8, who, "mean_x")) ||
+        (r = check_aligned(mean_y, 8, who, "mean_y")) ||
+        (r = check_aligned(moments, 8, who, "moments")))
+        return r;
     return launch_batch_finalize(acc, n_bunches, bunch_columns, counts, mean_x,
                                  mean_y, moments, moments_stride, nullptr,
                                  (cudaStream_t)stream);
@@ -472,6 +513,8 @@ int phk_wake_batch(const phk_wake_set* sets, int32_t n_bunches,
     if (n_kicks < 0 || n_kicks > PHK_MAX_KICKS)
         return set_error(PHK_ESIZE, "%s: n_kicks %d", who, n_kicks);
     if (n_kicks == 0) return PHK_OK;
+    int r = check_aligned(sets, 8, who, "sets");
+    if (r) return r;
     return launch_wake_batch(sets, n_bunches, n_slices, n_kicks,
                              (cudaStream_t)stream);
 }
@@ -521,6 +564,9 @@ int phk_wake_tc_expand(const phk_wake_tc* w, void* stream) {
     for (int g = 0; g < w->n_groups; ++g)
         if (!w->tables[g])
             return set_error(PHK_ENULL, "%s: table of group %d is NULL", who, g);
+    for (int g = 0; g < w->n_groups; ++g)
+        if ((r = check_aligned(w->tables[g], 8, who, "a group table")))
+            return r;
     return launch_wake_tc_expand(w, (cudaStream_t)stream);
 }
 
@@ -530,12 +576,17 @@ int phk_wake_tc_run(const phk_wake_tc* w, void* stream) {
     if (r) return r;
     if (!w->moments || !w->partials)
         return set_error(PHK_ENULL, "%s: moments / partials is NULL", who);
+    if ((r = check_aligned(w->moments, 8, who, "moments")) ||
+        (r = check_aligned(w->partials, 4, who, "partials")))
+        return r;
     if (w->ring_len < 1 || w->head < 0 || w->head >= w->ring_len)
         return set_error(PHK_EPARAM, "%s: ring_len %d head %d", who,
                          w->ring_len, w->head);
     if ((r = check_dtype(w->out_dtype, who))) return r;
     for (int k = 0; k < w->n_kicks; ++k) {
         if (!w->out[k]) return set_error(PHK_ENULL, "%s: out %d is NULL", who, k);
+        if ((r = check_aligned(w->out[k], dsize(w->out_dtype), who, "an output")))
+            return r;
         if (w->group_of[k] < 0 || w->group_of[k] >= w->n_groups)
             return set_error(PHK_EPARAM, "%s: kick %d group %d", who, k,
                              w->group_of[k]);

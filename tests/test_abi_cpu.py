@@ -386,3 +386,63 @@ def test_misaligned_tables_rejected_on_host(lib):
     assert L.phk_slice_moments(ctypes.byref(sl), 4096, 100, N.PHK_F64, q, 1,
                                0, None, sums, counts, None) == -3
     assert 'quantity' in N.last_error()
+
+
+def test_misaligned_buffers_of_merges_and_wakes_rejected_on_host(lib):
+    """Outputs and tables of the merges and wake convolutions: a pointer
+    not aligned to its element type is PHK_EALIGN on the host.  Every call
+    below fails validation, so none reaches a launch."""
+    from pyheadtail_gb300 import _native as N
+    L = N.load(build_if_missing=False)
+    acc = N.Accum()
+    acc.slicer.n_slices, acc.slicer.edges = 10, 65536
+    acc.partials, acc.grid, acc.partials_len = 131072 + 4, 1, 30
+    assert L.phk_slice_finalize(ctypes.byref(acc), 8192, 16384, 24576, None,
+                                None) == -3
+    assert 'partials' in N.last_error()
+    acc.partials = 131072
+    assert L.phk_slice_finalize(ctypes.byref(acc), 8192 + 2, 16384, 24576,
+                                None, None) == -3
+    assert 'counts' in N.last_error()
+    assert L.phk_slice_finalize(ctypes.byref(acc), 8192, 16384 + 4, 24576,
+                                None, None) == -3
+    assert L.phk_slice_finalize(ctypes.byref(acc), 8192, 16384, 24576,
+                                32768 + 4, None) == -3
+    assert 'moments_slot' in N.last_error()
+    assert L.phk_slice_merge(8192, 2, 10, 16384 + 2, 24576, 32768, None,
+                             None) == -3
+    assert L.phk_slice_merge(8192, 2, 10, 16384, 24576, 32768 + 4, None,
+                             None) == -3
+    assert L.phk_batch_finalize(ctypes.byref(acc), 2, 8192 + 2, 16384, 24576,
+                                32768, None, 0, None) == -3
+    assert 'bunch_columns' in N.last_error()
+
+    ws = N.WakeSet()
+    ws.n_slices, ws.ring_len, ws.head, ws.n_kicks = 10, 4, 0, 1
+    ws.out_dtype = N.PHK_F64
+    ws.moments = 8192 + 4
+    ws.kick[0].table, ws.kick[0].out = 16384, 24576
+    ws.kick[0].n_lags = 1
+    assert L.phk_wake(ctypes.byref(ws), None) == -3
+    assert 'moments' in N.last_error()
+    ws.moments = 8192
+    ws.kick[0].table = 16384 + 4
+    assert L.phk_wake(ctypes.byref(ws), None) == -3
+    ws.kick[0].table = 16384
+    ws.kick[0].out = 24576 + 4          # FP64 output, 4-byte aligned
+    assert L.phk_wake(ctypes.byref(ws), None) == -3
+    assert 'output' in N.last_error()
+    assert L.phk_wake_batch(8192 + 4, 2, 10, 1, None) == -3
+
+    prog = N.Program()
+    b = N.Batch()
+    b.n_bunches, b.n_units, b.n_columns, b.grid, b.threads = 1, 1, 1, 1, 256
+    b.units, b.cta_first, b.programs = 8192 + 4, 16384, 24576
+    b.programs_host = ctypes.pointer(prog)
+    c = N.Coords()
+    for i, f in enumerate(('x', 'xp', 'y', 'yp', 'z', 'dp')):
+        setattr(c, f, 65536 * (i + 1))
+    c.n, c.dtype = 100, N.PHK_F32
+    assert L.phk_track_batch(ctypes.byref(b), ctypes.byref(c), None, None,
+                             None) == -3
+    assert 'units' in N.last_error()
