@@ -624,6 +624,9 @@ int phk_charge_hist(const void* z, int64_t n, int32_t dtype, double tail,
     if (r) return r;
     if (!hist || !below)
         return set_error(PHK_ENULL, "%s: hist / below is NULL", who);
+    if ((r = check_aligned(hist, 4, who, "hist")) ||
+        (r = check_aligned(below, 8, who, "below")))
+        return r;
     if (n == 0) return PHK_OK;
     return launch_charge_hist(z, n, dtype, tail, head, K, hist,
                               reinterpret_cast<unsigned long long*>(below),
@@ -640,6 +643,13 @@ int phk_charge_gather(const void* z, int64_t n, int32_t dtype, double tail,
     if (r) return r;
     if (!seg_of_bin || !seg_off || !seg_count || !fill || !keys)
         return set_error(PHK_ENULL, "%s: a table is NULL", who);
+    if ((r = check_aligned(seg_of_bin, 4, who, "seg_of_bin")) ||
+        (r = check_aligned(seg_off, 8, who, "seg_off")) ||
+        (r = check_aligned(seg_count, 4, who, "seg_count")) ||
+        (r = check_aligned(fill, 4, who, "fill")) ||
+        (r = check_aligned(keys, 8, who, "keys")) ||
+        (r = check_aligned(status, 4, who, "status")))
+        return r;
     if (n == 0) return PHK_OK;
     return launch_charge_gather(z, n, dtype, tail, head, K, seg_of_bin,
                                 seg_off, seg_count, fill,
@@ -656,6 +666,15 @@ int phk_charge_select(const uint64_t* keys, const int64_t* seg_off,
     if (n_targets == 0) return PHK_OK;
     if (!keys || !seg_off || !seg_count || !tgt_seg || !tgt_rank || !out)
         return set_error(PHK_ENULL, "%s: a table is NULL", who);
+    int r;
+    if ((r = check_aligned(keys, 8, who, "keys")) ||
+        (r = check_aligned(seg_off, 8, who, "seg_off")) ||
+        (r = check_aligned(seg_count, 4, who, "seg_count")) ||
+        (r = check_aligned(tgt_seg, 4, who, "tgt_seg")) ||
+        (r = check_aligned(tgt_rank, 4, who, "tgt_rank")) ||
+        (r = check_aligned(out, 8, who, "out")) ||
+        (r = check_aligned(status, 4, who, "status")))
+        return r;
     return launch_charge_select(
         reinterpret_cast<const unsigned long long*>(keys), seg_off, seg_count,
         tgt_seg, tgt_rank, n_targets, out, status, (cudaStream_t)stream);

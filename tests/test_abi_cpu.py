@@ -446,3 +446,29 @@ def test_misaligned_buffers_of_merges_and_wakes_rejected_on_host(lib):
     assert L.phk_track_batch(ctypes.byref(b), ctypes.byref(c), None, None,
                              None) == -3
     assert 'units' in N.last_error()
+
+
+def test_misaligned_charge_slicer_tables_rejected_on_host(lib):
+    """Uniform-charge order statistics: histogram, key and segment tables
+    not aligned to their element type are PHK_EALIGN on the host (every
+    call below fails validation before a launch)."""
+    from pyheadtail_gb300 import _native as N
+    L = N.load(build_if_missing=False)
+    z = 4096
+    assert L.phk_charge_hist(z, 100, N.PHK_F64, -0.5, 0.5, 16, 8192 + 2,
+                             16384, None) == -3
+    assert L.phk_charge_hist(z, 100, N.PHK_F64, -0.5, 0.5, 16, 8192,
+                             16384 + 4, None) == -3
+    assert L.phk_charge_gather(z, 100, N.PHK_F64, -0.5, 0.5, 16, 8192,
+                               16384 + 4, 24576, 32768, 40960, 49152,
+                               None) == -3
+    assert 'seg_off' in N.last_error()
+    assert L.phk_charge_gather(z, 100, N.PHK_F64, -0.5, 0.5, 16, 8192,
+                               16384, 24576, 32768, 40960 + 4, 49152,
+                               None) == -3
+    assert 'keys' in N.last_error()
+    assert L.phk_charge_select(8192 + 4, 16384, 24576, 32768, 40960, 3,
+                               49152, 57344, None) == -3
+    assert L.phk_charge_select(8192, 16384, 24576, 32768, 40960, 3,
+                               49152 + 4, 57344, None) == -3
+    assert "out" in N.last_error()
