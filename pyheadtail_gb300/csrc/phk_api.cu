@@ -126,6 +126,8 @@ static int check_program(const phk_program* p, const char* who) {
     if (p->n_det < 0 || p->n_det > PHK_MAX_DETUNERS)
         return set_error(PHK_ESIZE, "%s: n_det %d outside [0, %d]", who,
                          p->n_det, PHK_MAX_DETUNERS);
+    if (reinterpret_cast<uintptr_t>(p->status) % 4)
+        return set_error(PHK_EALIGN, "%s: status word not 4-byte aligned", who);
     for (int o = 0; o < p->n_ops; ++o) {
         const phk_op& op = p->op[o];
         if (op.kind < PHK_OP_TRANSVERSE || op.kind > PHK_OP_DAMPER)
@@ -531,6 +533,8 @@ static int check_wake_tc(const phk_wake_tc* w, const char* who, bool planned) {
         if (w->group_lags[g] < 1 || w->group_lags[g] > 4096)
             return set_error(PHK_ESIZE, "%s: group %d lags %d", who, g,
                              w->group_lags[g]);
+    if (reinterpret_cast<uintptr_t>(w->status) % 4)
+        return set_error(PHK_EALIGN, "%s: status word not 4-byte aligned", who);
     if (!planned) return PHK_OK;
     phk_wake_tc p = *w;
     int64_t ae = 0, pe = 0;

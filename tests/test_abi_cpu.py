@@ -472,3 +472,26 @@ def test_misaligned_charge_slicer_tables_rejected_on_host(lib):
     assert L.phk_charge_select(8192, 16384, 24576, 32768, 40960, 3,
                                49152 + 4, 57344, None) == -3
     assert "out" in N.last_error()
+
+
+def test_misaligned_status_word_rejected_on_host(lib):
+    """The optional device status word of a program is updated with 32-bit
+    atomics: a pointer not aligned to 4 bytes is PHK_EALIGN on the host."""
+    from pyheadtail_gb300 import _native as N
+    L = N.load(build_if_missing=False)
+    prog = N.Program()
+    prog.status = 8192 + 2
+    c = N.Coords()
+    for i, f in enumerate(('x', 'xp', 'y', 'yp', 'z', 'dp')):
+        setattr(c, f, 4096 * (i + 1))
+    c.n, c.dtype = 100, N.PHK_F64
+    assert L.phk_track(ctypes.byref(prog), ctypes.byref(c), None, None,
+                       None) == -3
+    assert 'status' in N.last_error()
+    w = N.WakeTC()
+    w.n_slices, w.n_groups, w.n_kicks = 10, 1, 1
+    w.group_lags[0] = 2
+    w.status = 8192 + 2
+    a_el, p_el = ctypes.c_int64(), ctypes.c_int64()
+    assert L.phk_wake_tc_plan(ctypes.byref(w), ctypes.byref(a_el),
+                              ctypes.byref(p_el)) == -3
